@@ -1,0 +1,47 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+Compiles oracle/mbx_oracle.cpp into oracle/lib/libmbx_oracle.so with
+-ffp-contract=off (the restated operation order must be the executed order on
+every host, x86-64 and aarch64 alike) and, when the reference sources are
+present, the reference engine itself into oracle/_ref/ via ref_build/Makefile.
+"""
+import glob
+import os
+import platform
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "libmbx_oracle.so")
+REFERENCE = "/root/reference"
+
+
+def find_libgmp():
+    cands = glob.glob("/usr/lib/*-linux-gnu/libgmp.so.10") + glob.glob("/usr/lib64/libgmp.so.10") + glob.glob("/usr/lib/libgmp.so.10")
+    if not cands:
+        raise RuntimeError("libgmp.so.10 not found")
+    return cands[0]
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "mbx_oracle.cpp")
+    hdr = os.path.join(HERE, "oracle_gmp.h")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", LIB, find_libgmp()]
+    subprocess.check_call(cmd)
+    return LIB
+
+
+def build_reference():
+    """Compile the reference engine in place (x86-64 only; needs its sources)."""
+    if not os.path.isdir(os.path.join(REFERENCE, "src", "engine")) or platform.machine() not in ("x86_64", "AMD64"):
+        return None
+    subprocess.check_call(["make", "-s", "REF=" + REFERENCE], cwd=os.path.join(HERE, "ref_build"))
+    return os.path.join(HERE, "_ref", "mbx_refdump")
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_reference())
