@@ -1,0 +1,96 @@
+/* mbx_gb300.h — C ABI of the GB300 deep-zoom Mandelbrot perturbation renderer.
+ *
+ * Drop-in boundary for the reference's compute-backend plugin API
+ * (cbotx/Mandelbrot-Explorer src/engine/compute_backend.h). Plain C types only:
+ * pointers, sizes and a status code. One context owns one CUDA device, one
+ * stream and its device buffers; renders on one context are serialised.
+ * Reference citations below are file:line in that project.
+ */
+#ifndef MBX_GB300_H
+#define MBX_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBX_ABI_VERSION 1
+
+/* Coloring flags: same bit values as the reference's ColoringMethod enum
+ * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
+#define MBX_SUPER_SAMPLING 1
+#define MBX_EXTERIOR_DIST_EST 2
+#define MBX_DE_OVERLAY 64
+
+/* Arithmetic of the per-sample delta loop. */
+#define MBX_PRECISION_EXACT 0 /* FP64 / FP64-floatexp in the reference's exact operation order */
+#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration (floatexp frames only) */
+
+/* Status codes (the reference returns bool + ComputeBackendInfo strings). */
+#define MBX_OK 0
+#define MBX_E_INVALID (-1)     /* request failed validation (compute_backend.cpp:263-272) */
+#define MBX_E_CUDA (-2)        /* a CUDA call failed; see mbx_last_error */
+#define MBX_E_CANCELLED (-3)   /* mbx_cancel was called; outputs are partial (EMPTYPIXEL = -10) */
+#define MBX_E_NODEVICE (-4)    /* no usable CUDA device (there is no CPU fallback) */
+#define MBX_E_BUSY (-5)        /* another compute is active on this context */
+#define MBX_E_NOMEM (-6)       /* device or host allocation failed */
+
+typedef struct mbx_context mbx_context;
+
+/* One frame request. Mirrors ComputeRequest (src/engine/compute_backend.h:17-51)
+ * for ComputeMode::Mandelbrot with the view given as decimal strings instead of
+ * mpf_ptr, and the engine owned by the context instead of a Mandel*. */
+typedef struct {
+    const char* center_re;     /* view centre, decimal */
+    const char* center_im;
+    const char* scale;         /* reference scale: half-width = 2/scale (mp.cpp:1403-1416), decimal */
+    int precision_bits;        /* mpf precision; 0 => digits(scale)*log2(10)+64 (src/tools/render.cpp:170-174) */
+    int width, height;         /* base grid of this (strip) frame */
+    int full_height, row_base; /* strip rendering; 0 => whole frame (mp.cpp:1399-1424) */
+    int sub;                   /* odd sub-sample factor >= 1; buffers hold (width*sub) x (height*sub) */
+    int max_iterations;
+    int coloring_method;       /* MBX_* coloring flags */
+    double bailout;            /* escape radius; 0 => 1e8 (mp.h:283) */
+    int precision_mode;        /* MBX_PRECISION_* */
+    int outputs_on_device;     /* 1: the three output pointers are CUDA device pointers */
+    float* iterations;         /* required: smooth value / EDE distance / -2 interior / -10 empty */
+    float* normal;             /* optional: DE-overlay distance (MBX_DE_OVERLAY), else NULL */
+    int32_t* escape_iteration; /* optional: escape iteration N per sample, -1 interior, -10 empty */
+    volatile float* progress;  /* optional: 0..1 progress, written between passes */
+} mbx_request;
+
+typedef struct {
+    double total_ms, orbit_ms, bla_ms, kernel_ms, copy_ms;
+    long long steps;                /* executed delta-loop iterations */
+    long long bla_applies;          /* BLA skips taken */
+    long long bla_skipped;          /* iterations skipped by BLA */
+    long long effective_iterations; /* sum over samples of N (max_iterations for interior) */
+    long long gmp_pixels;           /* samples recomputed in arbitrary precision (mp.cpp:2173-2183) */
+    long long samples;              /* samples computed */
+    int passes, references, method, used_floatexp, period, reference_length, kernel_launches, interior;
+} mbx_stats;
+
+/* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns
+ * NULL with a message in err when no CUDA device is usable; never falls back. */
+mbx_context* mbx_create(int device, char* err, int err_len);
+void mbx_destroy(mbx_context* ctx);
+
+/* IComputeBackend::compute (src/engine/compute_backend.h:106-117, CPU version
+ * compute_backend.cpp:44-117). Synchronous; returns MBX_OK or a negative code. */
+int mbx_compute(mbx_context* ctx, const mbx_request* req, mbx_stats* stats);
+
+/* IComputeBackend::cancel / resetCancellation (compute_backend.cpp:119-128). Thread-safe. */
+void mbx_cancel(mbx_context* ctx);
+void mbx_reset_cancellation(mbx_context* ctx);
+
+/* ComputeBackendInfo (compute_backend.h:53-58): name/detail strings. */
+const char* mbx_info_name(const mbx_context* ctx);
+const char* mbx_info_detail(const mbx_context* ctx);
+const char* mbx_last_error(const mbx_context* ctx);
+int mbx_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

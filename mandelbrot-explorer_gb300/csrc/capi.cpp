@@ -1,0 +1,107 @@
+// extern "C" boundary (include/mbx_gb300.h). Validation mirrors the
+// reference's CpuComputeBackend::valid (src/engine/compute_backend.cpp:263-272)
+// plus the engine's own constraints (odd sub, mp.cpp:230).
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "engine.h"
+
+struct mbx_context {
+    mbx::Engine* engine = nullptr;
+    std::string name = "cuda";
+    std::string detail;
+    std::string last_error;
+    std::mutex mu;
+};
+
+namespace {
+// GMP keeps its default mpf precision in process-global state, which every
+// render sets; renders are therefore serialised process-wide.
+std::mutex g_gmp_mutex;
+
+int validate(const mbx_request* r, std::string& why) {
+    if (!r) {
+        why = "null request";
+        return MBX_E_INVALID;
+    }
+    const int full_h = r->full_height > 0 ? r->full_height : r->height;
+    if (!r->center_re || !r->center_im || !r->scale || !r->iterations) why = "missing centre, scale or iterations buffer";
+    else if (r->width < 2 || r->height < 1 || full_h < 2) why = "width must be >= 2 and the (full) height >= 2";
+    else if (r->row_base < 0 || r->row_base > full_h - r->height) why = "row_base outside the full frame";
+    else if (r->sub < 1 || (r->sub % 2) == 0 || r->sub > 255) why = "sub must be odd and in [1, 255]";
+    else if (r->max_iterations < 1) why = "max_iterations must be >= 1";
+    else if ((r->coloring_method & ~(MBX_SUPER_SAMPLING | MBX_EXTERIOR_DIST_EST | MBX_DE_OVERLAY)) != 0) why = "unsupported coloring_method bits";
+    else if (r->precision_mode != MBX_PRECISION_EXACT && r->precision_mode != MBX_PRECISION_MIXED) why = "unknown precision_mode";
+    else if (!(r->bailout >= 0.0) || r->bailout > 1e18) why = "bailout must be in [0, 1e18]";
+    else if ((long long)r->width * r->sub * r->height * r->sub > (1ll << 31) - 1) why = "frame too large";
+    else if (r->height >= (1 << 24) || r->width >= (1 << 24)) why = "dimensions too large";
+    else return MBX_OK;
+    return MBX_E_INVALID;
+}
+} // namespace
+
+extern "C" {
+
+int mbx_abi_version(void) { return MBX_ABI_VERSION; }
+
+mbx_context* mbx_create(int device, char* err, int err_len) {
+    auto fail = [&](const std::string& m) -> mbx_context* {
+        if (err && err_len > 0) {
+            strncpy(err, m.c_str(), (size_t)err_len - 1);
+            err[err_len - 1] = 0;
+        }
+        return nullptr;
+    };
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= device || device < 0) return fail(std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "index out of range"));
+    mbx_context* c = new (std::nothrow) mbx_context();
+    if (!c) return fail("out of memory");
+    c->engine = new (std::nothrow) mbx::Engine(device);
+    std::string why;
+    if (!c->engine || c->engine->init(why) != 0) {
+        delete c->engine;
+        delete c;
+        return fail("CUDA initialisation failed: " + why);
+    }
+    c->detail = std::string("GB300 perturbation renderer on ") + c->engine->device_name();
+    return c;
+}
+
+void mbx_destroy(mbx_context* c) {
+    if (!c) return;
+    delete c->engine;
+    delete c;
+}
+
+int mbx_compute(mbx_context* c, const mbx_request* r, mbx_stats* stats) {
+    if (!c) return MBX_E_INVALID;
+    std::string why;
+    int v = validate(r, why);
+    if (v != MBX_OK) {
+        std::lock_guard<std::mutex> l(c->mu);
+        c->last_error = why;
+        return v;
+    }
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    std::lock_guard<std::mutex> g(g_gmp_mutex);
+    int rc = c->engine->compute(*r, stats);
+    c->last_error = rc == MBX_OK ? std::string() : (c->engine->error().empty() ? std::string("compute failed") : c->engine->error());
+    if (rc == MBX_E_CANCELLED) c->last_error = "cancelled";
+    return rc;
+}
+
+void mbx_cancel(mbx_context* c) {
+    if (c && c->engine) c->engine->cancel();
+}
+void mbx_reset_cancellation(mbx_context* c) {
+    if (c && c->engine) c->engine->reset_cancel();
+}
+const char* mbx_info_name(const mbx_context* c) { return c ? c->name.c_str() : ""; }
+const char* mbx_info_detail(const mbx_context* c) { return c ? c->detail.c_str() : ""; }
+const char* mbx_last_error(const mbx_context* c) { return c ? c->last_error.c_str() : ""; }
+
+} // extern "C"

@@ -1,0 +1,202 @@
+// Host engine of the GB300 renderer (see engine.cpp).
+#pragma once
+#include <atomic>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "../../include/mbx_gb300.h"
+#include "gmp_abi.h"
+#include "kernels.h"
+
+namespace mbx {
+
+// The additive-feedback generator behind glibc's rand() (random_r TYPE_3,
+// degree 31, separation 3), seeded like srand(1). The reference picks a
+// fallback reference pixel with rand() (mp.cpp:4039-4052); a private replica
+// replays that sequence for every frame without touching the host's libc state.
+struct LibcRand {
+    int32_t st[31];
+    int f = 3, r = 0;
+    void seed(uint32_t s) {
+        if (s == 0) s = 1;
+        st[0] = (int32_t)s;
+        for (int i = 1; i < 31; ++i) {
+            int32_t hi = st[i - 1] / 127773, lo = st[i - 1] % 127773;
+            int32_t word = 16807 * lo - 2836 * hi;
+            if (word < 0) word += 2147483647;
+            st[i] = word;
+        }
+        f = 3;
+        r = 0;
+        for (int i = 0; i < 310; ++i) (void)next();
+    }
+    int next() {
+        uint32_t val = (uint32_t)st[f] + (uint32_t)st[r];
+        st[f] = (int32_t)val;
+        int out = (int)(val >> 1);
+        if (++f >= 31) {
+            f = 0;
+            ++r;
+        } else if (++r >= 31) {
+            r = 0;
+        }
+        return out;
+    }
+};
+
+// Fixed-point big real for the floatexp-path reference orbit (bigfixed.h).
+struct FixedReal {
+    int L = 0;
+    int sign = 0;
+    std::vector<uint64_t> limb;
+    void set_len(int l);
+    void from_mpf(mpf_srcptr x, int l);
+    void to_mpf(mpf_ptr out) const;
+    FE to_fe() const;
+    double to_double() const;
+    static void addsub(FixedReal& r, const FixedReal& a, int sa, const FixedReal& b, int sb);
+    static void mul(FixedReal& r, const FixedReal& a, const FixedReal& b, uint64_t* tmp);
+};
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+};
+
+int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_t prec, const std::atomic<bool>* cancel);
+bool newton_nucleus(mpf_ptr cr, mpf_ptr ci, int period, mp_bitcnt_t prec, int maxit);
+
+class Engine {
+  public:
+    explicit Engine(int device);
+    ~Engine();
+    int init(std::string& err);
+    int compute(const mbx_request& r, mbx_stats* st);
+    void cancel();
+    void reset_cancel();
+    const std::string& error() const { return err_; }
+    const char* device_name() const { return devname_; }
+
+  private:
+    int compute_frame(const mbx_request& r);
+    int render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int row_base, volatile float* progress);
+    int render_shallow(volatile float* progress);
+    int shallow_samples(const std::vector<uint64_t>& samples);
+    int glitch_loop(std::vector<uint64_t>& pending, int& ref_it, bool have, int* nr, volatile float* progress);
+    int supersample(int ref_it);
+    int run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it, bool* have_new_ref, int* new_ref);
+    cudaError_t run_mixed_pass(const DeviceFrame& f);
+    int prepare_mixed();
+    int recompute_gmp(const std::vector<int>& list, const std::function<void(int, int*)>& key_of);
+    int write_sample(const int* a, float v, int32_t n);
+    int flush_ref_value();
+
+    void set_precision(int p);
+    bool orbit_step(int i, int pr_it, bool past);
+    void sa_update(int i);
+    void reset_series();
+    float gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) const;
+    float gmp_sample(const int* a, int mxit, int* nout) const;
+    bool ref_tail_escapes(int last, int extra);
+    int build_reference(const int* pick, bool view_center);
+    int find_nucleus(int maxp);
+    int build_periodic_reference(int period);
+    FE nucleus_size() const;
+    int reference_for_frame();
+    int upload_reference(int ref_it);
+    int build_bla(int reflen);
+    int build_dc_tables();
+
+    DeviceFrame frame_view();
+    FrameGeom geom() const;
+    int cuda_ok(const char* what);
+    int fail_cuda(const char* what, cudaError_t e);
+    void release_device();
+    template <typename T>
+    bool ensure(DevBuf<T>& b, size_t n);
+
+    // device / context
+    int device_;
+    int nsm_ = 0;
+    char devname_[160] = {0};
+    cudaStream_t st_ = nullptr;
+    Counters* dctr_ = nullptr;
+    Counters* hctr_ = nullptr;
+    volatile int* hcancel_ = nullptr;
+    int* dcancel_ = nullptr;
+    std::atomic<bool> cancel_{false};
+    std::atomic<bool> active_{false};
+    std::string err_;
+    LibcRand rng_;
+    mbx_stats stats_{};
+
+    // frame configuration
+    int W_ = 0, H_ = 0, SUB_ = 1, MXIT_ = 0, cm_ = 0, mode_ = 0, method_ = 0;
+    bool deriv_ = false;
+    float escf_ = 1e8f;
+    double ESC2_ = 0.0;
+
+    // arbitrary-precision state
+    bool mpf_ready_ = false;
+    mpf_t c0_re_, c0_im_, dx_, dy_, scale_, ref_re_, ref_im_, t1_, t2_;
+    mpf_t zre_[2], zim_[2];
+    bool use_fixed_ = false;
+    int fixL_ = 0;
+    std::vector<uint64_t> ftmp_;
+    FixedReal fc_re_, fc_im_, fz_re_[2], fz_im_[2], ft1_, ft2_, fab_, fre_, fim_;
+    FE dfe_r_{1.0, 0}, dfe_i_{0.0, 0};
+
+    // reference orbit shadows (host staging)
+    std::vector<double2> hZ_, hD_;
+    std::vector<double> hzm3_;
+    std::vector<FE2> hZfe_;
+    int orbit_len_ = 0;
+
+    // series approximation
+    C2 sa_A_[kSaTerms], sa_B_[kSaTerms], sa_delta_{0, 0};
+    bool sa_valid_ = false;
+    int sa_it_ = 0, sa_order_ = 0;
+
+    // reference bookkeeping
+    int ref_[4] = {0, 0, 0, 0};
+    double ref_x_ = 0, ref_y_ = 0, ref_frac_re_ = 0, ref_frac_im_ = 0;
+    bool ref_virtual_ = false, ref_subpixel_ = false, ref_escaped_ = false;
+    int ref_period_ = 0, ref_escape_it_ = 0;
+    float ref_value_ = 0.0f, ref_value_store_ = 0.0f;
+    int32_t ref_n_ = -1, ref_n_store_ = -1;
+    bool ref_value_pending_ = false;
+
+    // engine switches (reference defaults, mp.cpp:1530-1588)
+    bool use_floatexp_ = false, fe_cutoff_sensitive_ = false, use_bla_ = true, use_interior_ = true;
+    int bla_minlevel_ = 3, interior_confirm_ = 4;
+    double interior_eps2_ = 9e-18;
+    FE dxfe_{0, 0}, dyfe_{0, 0};
+    BlaView bla_{};
+
+    // double-path spacing tables
+    std::vector<double> hdcx_, hdcy_;
+    int dc_xoff_ = 0, dc_yoff_ = 0;
+
+    // device buffers
+    DevBuf<double2> dZ_, dD_;
+    DevBuf<FE2> dZfe_;
+    DevBuf<double> dzm3_, dr2_, ddcx_, ddcy_, dglitch_;
+    DevBuf<double4> dab_, dce_;
+    DevBuf<float> diter_own_, dnormal_own_;
+    DevBuf<int32_t> descN_own_;
+    DevBuf<uint64_t> dkeys_;
+    DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
+    DevBuf<float2> dZf_;
+    float* out_iter_ = nullptr;
+    float* out_norm_ = nullptr;
+    int32_t* out_n_ = nullptr;
+
+    // pass readback
+    std::vector<uint8_t> hdone_, hgmp_;
+    std::vector<double> hglitch_;
+    std::vector<uint64_t> grid_pending_;
+};
+
+} // namespace mbx

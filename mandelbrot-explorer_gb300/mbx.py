@@ -1,0 +1,310 @@
+"""Host-side mirror of the reference's compute-backend plugin API over the C ABI.
+
+The reference selects a renderer with ``createComputeBackend(name)`` and calls
+``IComputeBackend::compute(const ComputeRequest&)`` (cbotx/Mandelbrot-Explorer
+src/engine/compute_backend.h:17-117). This module exposes the same names and
+argument meanings for the "cuda" backend implemented by
+``lib/libmbx_gb300.so`` (declared in ``include/mbx_gb300.h``):
+
+    backend = create_compute_backend("cuda")
+    req = ComputeRequest(center_re="-0.75", center_im="0.1", scale="2" + "0"*30,
+                         width=1280, height=720, max_iterations=50000)
+    ok = backend.compute(req)          # fills req.iterations (numpy float32)
+
+There is no CPU fallback: when the library or a CUDA device is unavailable,
+``create_compute_backend`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmbx_gb300.so")
+
+# ColoringMethod bits (src/engine/mandel_perturbation.h:30-49).
+SUPER_SAMPLING = 1
+EXTERIOR_DIST_EST = 2
+DE_OVERLAY = 64
+EMPTYPIXEL = -10.0
+
+PRECISION_EXACT = 0
+PRECISION_MIXED = 1
+
+OK, E_INVALID, E_CUDA, E_CANCELLED, E_NODEVICE, E_BUSY, E_NOMEM = 0, -1, -2, -3, -4, -5, -6
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [
+        ("center_re", ctypes.c_char_p),
+        ("center_im", ctypes.c_char_p),
+        ("scale", ctypes.c_char_p),
+        ("precision_bits", ctypes.c_int),
+        ("width", ctypes.c_int),
+        ("height", ctypes.c_int),
+        ("full_height", ctypes.c_int),
+        ("row_base", ctypes.c_int),
+        ("sub", ctypes.c_int),
+        ("max_iterations", ctypes.c_int),
+        ("coloring_method", ctypes.c_int),
+        ("bailout", ctypes.c_double),
+        ("precision_mode", ctypes.c_int),
+        ("outputs_on_device", ctypes.c_int),
+        ("iterations", ctypes.c_void_p),
+        ("normal", ctypes.c_void_p),
+        ("escape_iteration", ctypes.c_void_p),
+        ("progress", ctypes.c_void_p),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("total_ms", ctypes.c_double),
+        ("orbit_ms", ctypes.c_double),
+        ("bla_ms", ctypes.c_double),
+        ("kernel_ms", ctypes.c_double),
+        ("copy_ms", ctypes.c_double),
+        ("steps", ctypes.c_longlong),
+        ("bla_applies", ctypes.c_longlong),
+        ("bla_skipped", ctypes.c_longlong),
+        ("effective_iterations", ctypes.c_longlong),
+        ("gmp_pixels", ctypes.c_longlong),
+        ("samples", ctypes.c_longlong),
+        ("passes", ctypes.c_int),
+        ("references", ctypes.c_int),
+        ("method", ctypes.c_int),
+        ("used_floatexp", ctypes.c_int),
+        ("period", ctypes.c_int),
+        ("reference_length", ctypes.c_int),
+        ("kernel_launches", ctypes.c_int),
+        ("interior", ctypes.c_int),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every symbol declared in include/mbx_gb300.h.
+EXPORTS = (
+    "mbx_create",
+    "mbx_destroy",
+    "mbx_compute",
+    "mbx_cancel",
+    "mbx_reset_cancellation",
+    "mbx_info_name",
+    "mbx_info_detail",
+    "mbx_last_error",
+    "mbx_abi_version",
+)
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load_library(path: Optional[str] = None, build_if_missing: bool = True):
+    """Load libmbx_gb300.so (building it in-tree if absent); raises on failure."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p) and build_if_missing:
+            import importlib.util
+
+            spec = importlib.util.spec_from_file_location("mbx_build", os.path.join(HERE, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build()
+        lib = ctypes.CDLL(p)
+        lib.mbx_create.restype = ctypes.c_void_p
+        lib.mbx_create.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+        lib.mbx_destroy.argtypes = [ctypes.c_void_p]
+        lib.mbx_compute.restype = ctypes.c_int
+        lib.mbx_compute.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Stats)]
+        lib.mbx_cancel.argtypes = [ctypes.c_void_p]
+        lib.mbx_reset_cancellation.argtypes = [ctypes.c_void_p]
+        for fn in ("mbx_info_name", "mbx_info_detail", "mbx_last_error"):
+            getattr(lib, fn).restype = ctypes.c_char_p
+            getattr(lib, fn).argtypes = [ctypes.c_void_p]
+        lib.mbx_abi_version.restype = ctypes.c_int
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def precision_for_scale(scale: str) -> int:
+    """render.cpp:170-174 / verify.cpp runCase: bits = digits(scale)*log2(10)+64."""
+    digits = sum(ch.isdigit() for ch in scale)
+    return int(digits * math.log(10) / math.log(2)) + 64
+
+
+def scale_digits(exponent: int, mantissa: str = "1") -> str:
+    """Decimal digit string for mantissa * 10**exponent (the reference tools' scale form)."""
+    return mantissa + "0" * exponent
+
+
+@dataclass
+class ComputeBackendInfo:
+    """compute_backend.h:53-58."""
+
+    name: str
+    detail: str
+    hardware_accelerated: bool = True
+    fallback: bool = False
+
+
+@dataclass
+class ComputeRequest:
+    """ComputeRequest (compute_backend.h:17-51), Mandelbrot mode.
+
+    ``scale`` is the reference's mpf scale as a decimal string: the view
+    half-width is 2/scale. Output buffers are allocated when left None:
+    ``iterations`` (float32, reference layout), ``normal`` (DE overlay) and
+    ``escape_iteration`` (int32 N per sample, -1 interior, -10 empty).
+    Passing torch CUDA tensors keeps the outputs on the device.
+    """
+
+    center_re: str
+    center_im: str
+    scale: str
+    width: int
+    height: int
+    max_iterations: int
+    sub: int = 1
+    coloring_method: int = 0
+    full_height: int = 0
+    row_base: int = 0
+    bailout: float = 1e8
+    precision_bits: int = 0
+    precision_mode: int = PRECISION_EXACT
+    iterations: object = None
+    normal: object = None
+    escape_iteration: object = None
+    want_escape_iteration: bool = True
+    progress: Optional[ctypes.c_float] = None
+
+    def sample_count(self) -> int:
+        return self.width * self.height * self.sub * self.sub
+
+
+class CudaComputeBackend:
+    """IComputeBackend (compute_backend.h:106-117) for the GB300 renderer."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        err = ctypes.create_string_buffer(512)
+        ctx = self._lib.mbx_create(device, err, 512)
+        if not ctx:
+            raise RuntimeError("CUDA backend unavailable: " + err.value.decode(errors="replace"))
+        self._ctx = ctypes.c_void_p(ctx)
+        self.last_stats = Stats()
+        self.last_status = OK
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.mbx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> ComputeBackendInfo:
+        return ComputeBackendInfo(self._lib.mbx_info_name(self._ctx).decode(), self._lib.mbx_info_detail(self._ctx).decode())
+
+    def last_compute_used_gpu_path(self) -> bool:
+        return True
+
+    def last_error(self) -> str:
+        return self._lib.mbx_last_error(self._ctx).decode(errors="replace")
+
+    def cancel(self):
+        self._lib.mbx_cancel(self._ctx)
+
+    def reset_cancellation(self):
+        self._lib.mbx_reset_cancellation(self._ctx)
+
+    @staticmethod
+    def _ptr(buf):
+        if buf is None:
+            return None, False
+        if isinstance(buf, np.ndarray):
+            if not buf.flags["C_CONTIGUOUS"]:
+                raise ValueError("output buffers must be contiguous")
+            return buf.ctypes.data, False
+        if hasattr(buf, "data_ptr") and getattr(buf, "is_cuda", False):
+            return buf.data_ptr(), True
+        raise TypeError("output buffers must be numpy arrays or torch CUDA tensors")
+
+    def compute_status(self, req: ComputeRequest) -> int:
+        n = req.sample_count()
+        if req.iterations is None:
+            req.iterations = np.empty(n, np.float32)
+        if req.normal is None and (req.coloring_method & DE_OVERLAY):
+            req.normal = np.empty(n, np.float32)
+        if req.escape_iteration is None and req.want_escape_iteration and isinstance(req.iterations, np.ndarray):
+            req.escape_iteration = np.empty(n, np.int32)
+        it, dev = self._ptr(req.iterations)
+        nr, dev2 = self._ptr(req.normal)
+        en, dev3 = self._ptr(req.escape_iteration)
+        flags = {d for d, p in ((dev, it), (dev2, nr), (dev3, en)) if p is not None}
+        if len(flags) > 1:
+            raise ValueError("output buffers must all be host arrays or all be CUDA tensors")
+        r = _Request(
+            req.center_re.encode(),
+            req.center_im.encode(),
+            req.scale.encode(),
+            req.precision_bits,
+            req.width,
+            req.height,
+            req.full_height,
+            req.row_base,
+            req.sub,
+            req.max_iterations,
+            req.coloring_method,
+            float(req.bailout),
+            req.precision_mode,
+            1 if dev else 0,
+            it,
+            nr,
+            en,
+            ctypes.cast(ctypes.pointer(req.progress), ctypes.c_void_p) if req.progress is not None else None,
+        )
+        st = Stats()
+        rc = self._lib.mbx_compute(self._ctx, ctypes.byref(r), ctypes.byref(st))
+        self.last_stats = st
+        self.last_status = rc
+        return rc
+
+    def compute(self, req: ComputeRequest) -> bool:
+        """True on success, like IComputeBackend::compute."""
+        return self.compute_status(req) == OK
+
+
+def create_compute_backend(requested: str = "cuda", device: int = 0) -> CudaComputeBackend:
+    """createComputeBackend (compute_backend.cpp:277-290) — only "cuda"/"gpu" exist here."""
+    name = (requested or "cuda").lower()
+    if name not in ("cuda", "gpu", "gb300", "auto"):
+        raise ValueError("unknown backend %r (this library provides only the CUDA backend)" % requested)
+    return CudaComputeBackend(device)
+
+
+def render(center_re, center_im, scale, width, height, max_iterations, **kw):
+    """One-call convenience: returns (iterations, normal, escape_iteration, stats)."""
+    be = create_compute_backend("cuda", kw.pop("device", 0))
+    try:
+        req = ComputeRequest(center_re, center_im, scale, width, height, max_iterations, **kw)
+        rc = be.compute_status(req)
+        if rc != OK:
+            raise RuntimeError("mbx_compute failed (%d): %s" % (rc, be.last_error()))
+        return req.iterations, req.normal, req.escape_iteration, be.last_stats.as_dict()
+    finally:
+        be.close()

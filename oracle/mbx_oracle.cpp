@@ -347,8 +347,8 @@ struct Pix {
 
 class Engine {
   public:
-    Engine(int w, int h, int mxit, int sub, float* iter, float* normal, double bailout, const Opts& o)
-        : W(w), H(h), MXIT(mxit), SUB(sub), iter_(iter), normal_(normal), opt(o) {
+    Engine(int w, int h, int mxit, int sub, float* iter, float* normal, int32_t* escn, double bailout, const Opts& o)
+        : W(w), H(h), MXIT(mxit), SUB(sub), iter_(iter), normal_(normal), escn_(escn), opt(o) {
         escf = (float)bailout;
         ESC2 = (double)(escf * escf); // mp.h:115-118: float*float, widened
         zfr.resize(MXIT + 1);
@@ -382,6 +382,7 @@ class Engine {
     const int W, H, MXIT, SUB;
     float* iter_;
     float* normal_;
+    int32_t* escn_; // escape iteration N per sample (instrumentation; -1 interior)
     Opts opt;
     float escf;
     double ESC2;
@@ -421,13 +422,16 @@ class Engine {
     int idx(const Pix& p) const { // mp.cpp:4334-4340
         return (p.a[0] * SUB + SUB / 2 + p.a[2]) * W * SUB + (p.a[1] * SUB + SUB / 2 + p.a[3]);
     }
-    void setPixel(const Pix& p, float v) { iter_[idx(p)] = v; }
+    void setPixel(const Pix& p, float v, int n) {
+        iter_[idx(p)] = v;
+        if (escn_) escn_[idx(p)] = n;
+    }
     static bool deriv_of(int cm) { return (cm & (CM_EDE | CM_DEOVL)) != 0; }
 
-    double floatPoint(double c_re, double c_im, int mxit, int cm, double* nrm) const;
-    float shallowSimd(double cr, double ci, int mxit, int cm) const;
-    float accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm) const;
-    float accuratePixel(const Pix& p, int mxit, int cm) const;
+    double floatPoint(double c_re, double c_im, int mxit, int cm, double* nrm, int* nout = nullptr) const;
+    float shallowSimd(double cr, double ci, int mxit, int cm, int* nout = nullptr) const;
+    float accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, int* nout = nullptr) const;
+    float accuratePixel(const Pix& p, int mxit, int cm, int* nout = nullptr) const;
     bool refTailEscapes(int last, int extra) const;
     int findNucleus(mpf_ptr nre, mpf_ptr nim, int maxp);
     int createPeriodicRef(int period, int cm);
@@ -439,15 +443,16 @@ class Engine {
     void buildBLA(int reflen, bool ede);
     int tryBLA(int s, double& dzr, double& dzi, double& ddr, double& ddi, double dcr, double dci, bool ede, int mx_ref_it) const;
     int tryBLAfe(int s, FE& S, FE S2, double& wr, double& wi, double dr, double di, int mx_ref_it, double* ab) const;
-    float pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, float* nrm) const;
-    float rescaledNoBla(FE dcr, FE dci, int mx_ref_it, int mxit) const;
+    float pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, float* nrm, int* nout) const;
+    float rescaledNoBla(FE dcr, FE dci, int mx_ref_it, int mxit, int* nout) const;
     void stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mxit, int cm, const std::vector<std::array<int, 4>>* contiguous = nullptr);
 };
 
 static inline Pix P(const std::array<int, 4>& a) { return Pix{{a[0], a[1], a[2], a[3]}}; }
 
 // mp.cpp:330-399 (smooth / EDE / DE-overlay branches).
-double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nrm) const {
+double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nrm, int* nout) const {
+    if (nout) *nout = -1;
     double z_re = c_re, z_im = c_im, d_re = 2, d_im = 0, dc_re = 1, dc_im = 0, tmp;
     const bool de_ovl = (cm & CM_DEOVL) != 0;
     const bool deriv = (cm & CM_EDE) || de_ovl;
@@ -466,6 +471,7 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
         z_re = tmp;
         tmp = z_re * z_re + z_im * z_im;
         if (tmp > ESC2) {
+            if (nout) *nout = i + 1;
             if (cm & CM_EDE) return std::sqrt(tmp) * std::log(tmp) / std::sqrt(dc_re * dc_re + dc_im * dc_im);
             if (de_ovl) {
                 if (nrm) *nrm = std::sqrt(tmp) * std::log(tmp) / std::sqrt(dc_re * dc_re + dc_im * dc_im);
@@ -481,7 +487,8 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
 }
 
 // mp.cpp:416-532 for one pixel (lane refill does not change per-pixel values).
-float Engine::shallowSimd(double cr, double ci, int mxit, int cm) const {
+float Engine::shallowSimd(double cr, double ci, int mxit, int cm, int* nout) const {
+    if (nout) *nout = -1;
     const bool ede = (cm & CM_EDE) != 0;
     const double LG2 = std::log(2.0);
     double zr = cr, zi = ci, dr = 2, di = 0, dcr = 1, dci = 0, jv = 1;
@@ -497,6 +504,7 @@ float Engine::shallowSimd(double cr, double ci, int mxit, int cm) const {
         double dmag = (dr * dr) + (di * di);
         double jnext = jv + 1.0;
         if (zrad > ESC2) {
+            if (nout) *nout = (int)jv + 1;
             if (ede) return (float)(std::sqrt(zrad) * std::log(zrad) / std::sqrt(dcr * dcr + dci * dci));
             return (float)(jv + 1 - std::log(std::log(zrad) / 2 / LG2) / LG2);
         }
@@ -507,7 +515,8 @@ float Engine::shallowSimd(double cr, double ci, int mxit, int cm) const {
 }
 
 // mp.cpp:719-894 (smooth / EDE branches; derivative tracked, no env overrides).
-float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm) const {
+float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, int* nout) const {
+    if (nout) *nout = -1;
     const mp_bitcnt_t wp = mpf_get_prec(c_re);
     mpf_t tt1, tt2, z_re, z_im, d_re, d_im, dc_re, dc_im, e1, e2;
     mpf_init2(tt1, wp); mpf_init2(tt2, wp);
@@ -552,6 +561,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm) 
         mpf_add(tt1, tt1, tt2);
         double rad = mpf_get_d(tt1);
         if (rad > ESC2) {
+            if (nout) *nout = i + 1;
             if (ede) {
                 mpf_mul(e1, dc_re, dc_re);
                 mpf_mul(e2, dc_im, dc_im);
@@ -583,7 +593,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm) 
 }
 
 // mp.cpp:896-919.
-float Engine::accuratePixel(const Pix& p, int mxit, int cm) const {
+float Engine::accuratePixel(const Pix& p, int mxit, int cm, int* nout) const {
     mpf_t cre, cim, off, soff;
     mpf_init(cre); mpf_set(cre, c0_re);
     mpf_init(cim); mpf_set(cim, c0_im);
@@ -602,7 +612,7 @@ float Engine::accuratePixel(const Pix& p, int mxit, int cm) const {
     if (p.a[2] < 0) mpf_neg(soff, soff);
     mpf_div_ui(soff, soff, SUB);
     mpf_add(cim, cim, soff);
-    float r = accuratePoint(cre, cim, mxit, cm);
+    float r = accuratePoint(cre, cim, mxit, cm, nout);
     mpf_clears(cre, cim, off, soff, (mpf_ptr)0);
     return r;
 }
@@ -1019,7 +1029,9 @@ int Engine::createRef(std::set<std::array<int, 4>>& s, int pr_it, int mxit, bool
             if (ref_virtual && use_floatexp && i >= mxit - 16) fe_cutoff_sensitive = true;
             if (!ref_virtual) {
                 if (cm) {
-                    setPixel(ref_, accuratePoint(ref_re, ref_im, mxit, cm));
+                    int nn;
+                    float rv = accuratePoint(ref_re, ref_im, mxit, cm, &nn);
+                    setPixel(ref_, rv, nn);
                 } else {
                     if (use_bigfixed) {
                         bf_to_mpf(zre[i & 1], bz_re[i & 1]);
@@ -1029,14 +1041,14 @@ int Engine::createRef(std::set<std::array<int, 4>>& s, int pr_it, int mxit, bool
                     mpf_mul(t2, zim[i & 1], zim[i & 1]);
                     mpf_add(t1, t1, t2);
                     double rad = mpf_get_d(t1);
-                    setPixel(ref_, (float)(i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2)));
+                    setPixel(ref_, (float)(i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2)), i + 1);
                 }
             }
             return i;
         }
     }
     if (ref_virtual && use_floatexp) fe_cutoff_sensitive = accuratePoint(ref_re, ref_im, mxit + 64, cm) >= 0;
-    if (!ref_virtual) setPixel(ref_, -2.f);
+    if (!ref_virtual) setPixel(ref_, -2.f, -1);
     return mxit;
 }
 
@@ -1417,7 +1429,8 @@ int Engine::tryBLAfe(int s, FE& S, FE S2, double& wr, double& wi, double dr, dou
 }
 
 // mp.cpp:3287-3618 (smooth / EDE / DE-overlay; no stripe or trap accumulators).
-float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, float* nrm) const {
+float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, float* nrm, int* nout) const {
+    *nout = -1;
     const double LG2 = std::log(2.0);
     const int reflen = mx_ref_it + 1;
     const int per = ref_period;
@@ -1560,6 +1573,7 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
         double zr = Xr + s * wr, zi = Xi + s * wi;
         double zrad = zr * zr + zi * zi;
         if (zrad > ESC2) {
+            *nout = iter;
             if (ede) {
                 double num = std::sqrt(zrad) * std::log(zrad);
                 FE Jmag = fe_mul_d(SJ, std::sqrt(jr * jr + ji * ji));
@@ -1651,7 +1665,8 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
 }
 
 // mp.cpp:3620-3816 for one lane (lanes are independent).
-float Engine::rescaledNoBla(FE dcr, FE dci, int mx_ref_it, int mxit) const {
+float Engine::rescaledNoBla(FE dcr, FE dci, int mx_ref_it, int mxit, int* nout) const {
+    *nout = -1;
     const double logTwo = std::log(2.0);
     const int referenceLength = mx_ref_it + 1;
     double wr = 0, wi = 0, sd, dr = 0, di = 0;
@@ -1709,7 +1724,10 @@ float Engine::rescaledNoBla(FE dcr, FE dci, int mx_ref_it, int mxit) const {
         }
         ++index;
         ++iteration;
-        if (actual > ESC2) return static_cast<float>(static_cast<double>(iteration) - std::log(std::log(actual) / 2.0 / logTwo) / logTwo);
+        if (actual > ESC2) {
+            *nout = iteration;
+            return static_cast<float>(static_cast<double>(iteration) - std::log(std::log(actual) / 2.0 / logTwo) / logTwo);
+        }
         if (delta > 1e16 || (delta < 1e-16 && delta > 0.0)) {
             const FE nm = fe_sqrt(fe_from(delta));
             scale = fe_mul(scale, nm);
@@ -1769,12 +1787,13 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
             FE Dcr = fe_mul_d(dxfe, px - ref_x);
             FE Dci = fe_mul_d(dyfe, py - ref_y);
             float nrm = 0.0f;
-            float value = noBla ? rescaledNoBla(Dcr, Dci, mx_ref_it, mxit) : pixelRescaled(Dcr, Dci, mx_ref_it, mxit, cm, de_ovl ? &nrm : nullptr);
+            int nn = -1;
+            float value = noBla ? rescaledNoBla(Dcr, Dci, mx_ref_it, mxit, &nn) : pixelRescaled(Dcr, Dci, mx_ref_it, mxit, cm, de_ovl ? &nrm : nullptr, &nn);
             if (value == EMPTY || (fe_cutoff_sensitive && (value < 0 || value > mxit - 16))) {
-                value = accuratePixel(arr, mxit, cm);
+                value = accuratePixel(arr, mxit, cm, &nn);
                 ++gmp;
             }
-            setPixel(arr, value);
+            setPixel(arr, value, nn);
             if (de_ovl && normal_) normal_[idx(arr)] = nrm;
             done[i] = 1;
         }
@@ -1838,7 +1857,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
         while (j < mxit) {
             if (int_rep) {
                 if (k == sk && dzr == sdzr && dzi == sdzi) {
-                    setPixel(arr, -2);
+                    setPixel(arr, -2, -1);
                     done[i] = 1;
                     fin = true;
                     break;
@@ -1904,12 +1923,12 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                 rk = k;
             if (zrad > ESC2) {
                 if (ede) {
-                    setPixel(arr, std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di));
+                    setPixel(arr, std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di), j + 1);
                 } else if (de_ovl) {
-                    setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2));
+                    setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
                     if (normal_) normal_[idx(arr)] = (float)(std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di));
                 } else {
-                    setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2));
+                    setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
                 }
                 done[i] = 1;
                 fin = true;
@@ -1924,7 +1943,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                         bool ret = (pr * pr + pi * pi < interior_eps2 * zrad);
                         if (ret && conf_D2 < 1.0) {
                             if (++conf_count >= interior_confirm) {
-                                setPixel(arr, -2);
+                                setPixel(arr, -2, -1);
                                 done[i] = 1;
                                 fin = true;
                                 break;
@@ -1982,7 +2001,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
         }
         (void)fin;
         if (j >= mxit) {
-            setPixel(arr, -2);
+            setPixel(arr, -2, -1);
             done[i] = 1;
         }
     }
@@ -2040,13 +2059,16 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
             double cim = c0i + dyf * i;
             for (int j = 0; j < W; ++j) {
                 Pix p{{i, j, 0, 0}};
+                int nn = -1;
                 if (!deovl) {
-                    double val = shallowSimd(c0r + dxf * j, cim, mxit, cm);
+                    double val = shallowSimd(c0r + dxf * j, cim, mxit, cm, &nn);
                     if (ede && val >= 0) val /= dxf;
                     iter_[idx(p)] = (float)val;
+                    if (escn_) escn_[idx(p)] = nn;
                 } else {
                     double de = 0.0;
-                    iter_[idx(p)] = (float)floatPoint(c0r + dxf * j, cim, mxit, cm, &de);
+                    iter_[idx(p)] = (float)floatPoint(c0r + dxf * j, cim, mxit, cm, &de, &nn);
+                    if (escn_) escn_[idx(p)] = nn;
                     if (normal_) normal_[idx(p)] = (iter_[idx(p)] < 0) ? 0.0f : (float)(de / dxf);
                 }
             }
@@ -2134,9 +2156,10 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
                     double ci = c0i + dyf * v[q][0] + dyf * yi / SUB;
                     // sub^2 <= 128 takes the lane-refill kernel (float result), larger
                     // sub the scalar floatPointCompute (double result) (mp.cpp:1936-1967).
-                    double it = (SUB * SUB <= 128) ? (double)shallowSimd(cr, ci, mxit, cm) : floatPoint(cr, ci, mxit, cm & CM_EDE, nullptr);
+                    int nn = -1;
+                    double it = (SUB * SUB <= 128) ? (double)shallowSimd(cr, ci, mxit, cm, &nn) : floatPoint(cr, ci, mxit, cm & CM_EDE, nullptr, &nn);
                     if (ede && it >= 0) it /= dxf;
-                    setPixel(Pix{{v[q][0], v[q][1], yi, xi}}, (float)it);
+                    setPixel(Pix{{v[q][0], v[q][1], yi, xi}}, (float)it, nn);
                 }
         }
         return;
@@ -2172,8 +2195,10 @@ extern "C" {
 // mpf_set_default_prec(prec). iter/normal hold (W*sub)*(H*sub) floats and are
 // filled with EMPTYPIXEL / 0 first. stats (optional, 8 slots): executed delta
 // steps, BLA applies, BLA-skipped iterations, passes, references built, GMP
-// per-pixel recomputations, method (0 shallow / 1 perturbation).
-int mbx_oracle_render(const char* cx, const char* cy, const char* scale_digits, int prec_bits, int W, int H, int mxit, int sub, int cmethod, double bailout, int full_h, int row_base, int threads, float* iter, float* normal, long long* stats) {
+// per-pixel recomputations, method (0 shallow / 1 perturbation). escn
+// (optional) receives each sample's escape iteration N (-1 interior), an
+// instrumentation output with no counterpart in the reference.
+int mbx_oracle_render(const char* cx, const char* cy, const char* scale_digits, int prec_bits, int W, int H, int mxit, int sub, int cmethod, double bailout, int full_h, int row_base, int threads, float* iter, float* normal, int32_t* escn, long long* stats) {
     if (W < 2 || H < 1 || mxit < 1 || sub < 1 || (sub % 2) == 0 || !iter) return -1;
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
@@ -2182,6 +2207,8 @@ int mbx_oracle_render(const char* cx, const char* cy, const char* scale_digits, 
     for (size_t i = 0; i < n; ++i) iter[i] = EMPTY;
     if (normal)
         for (size_t i = 0; i < n; ++i) normal[i] = 0.0f;
+    if (escn)
+        for (size_t i = 0; i < n; ++i) escn[i] = -10;
     mpf_set_default_prec((mp_bitcnt_t)prec_bits);
     mpf_t mcx, mcy, msc;
     mpf_init_set_str(mcx, cx, 10);
@@ -2189,7 +2216,7 @@ int mbx_oracle_render(const char* cx, const char* cy, const char* scale_digits, 
     mpf_init_set_str(msc, scale_digits, 10);
     Opts o;
     {
-        Engine e(W, H, mxit, sub, iter, normal, bailout, o);
+        Engine e(W, H, mxit, sub, iter, normal, escn, bailout, o);
         e.setPrecision(prec_bits);
         e.compute(mcx, mcy, msc, mxit, cmethod, full_h, row_base);
         if (stats) {

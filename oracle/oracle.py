@@ -1,0 +1,49 @@
+"""ORACLE — test infrastructure only (tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py). Python access to oracle/lib/libmbx_oracle.so, the CPU
+restatement of the reference's perturbation path (mbx_oracle.cpp).
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(HERE, "build_oracle.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        path = mod.build_oracle()
+        lib = ctypes.CDLL(path)
+        lib.mbx_oracle_render.restype = ctypes.c_int
+        lib.mbx_oracle_render.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 6 + [ctypes.c_double] + [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4
+        _lib = lib
+    return _lib
+
+
+def precision_for_scale(scale):
+    return int(sum(ch.isdigit() for ch in scale) * math.log(10) / math.log(2)) + 64
+
+
+def render(center_re, center_im, scale, width, height, max_iterations, sub=1, coloring_method=0, bailout=1e8, full_height=0, row_base=0, threads=0, precision_bits=0):
+    """Returns (iterations float32, normal float32, escape iteration int32, stats dict)."""
+    lib = load()
+    n = width * height * sub * sub
+    it = np.empty(n, np.float32)
+    nr = np.empty(n, np.float32)
+    en = np.empty(n, np.int32)
+    st = np.zeros(8, np.int64)
+    lib.mbx_oracle_reset_rand()
+    prec = precision_bits or precision_for_scale(scale)
+    rc = lib.mbx_oracle_render(center_re.encode(), center_im.encode(), scale.encode(), prec, width, height, max_iterations, sub, coloring_method, float(bailout), full_height, row_base, threads, it.ctypes.data, nr.ctypes.data, en.ctypes.data, st.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle rejected the request (%d)" % rc)
+    keys = ("steps", "bla_applies", "bla_skipped", "passes", "references", "gmp_pixels", "method")
+    return it, nr, en, dict(zip(keys, (int(x) for x in st)))

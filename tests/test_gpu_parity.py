@@ -1,0 +1,104 @@
+"""CUDA renderer (exact form) against the oracle and the reference fixtures.
+
+Bar: class (interior / exterior / empty) and escape iteration N identical for
+every sample; smooth value / distance within 1e-6 relative (the only allowed
+difference is the last-ulp behaviour of log on the GPU vs the host libm).
+"""
+import numpy as np
+import pytest
+
+import mbx
+import oracle
+from conftest import load_cases, load_fixture
+
+CASES = load_cases()
+pytestmark = pytest.mark.gpu
+RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def backend():
+    be = mbx.create_compute_backend("cuda")
+    yield be
+    be.close()
+
+
+def gpu_render(be, c, **kw):
+    req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"], **kw)
+    rc = be.compute_status(req)
+    assert rc == mbx.OK, be.last_error()
+    return req.iterations, req.normal, req.escape_iteration, be.last_stats.as_dict()
+
+
+def assert_same(it, en, ref_it, ref_en, label):
+    assert np.array_equal(it == -10.0, ref_it == -10.0), label + ": empty samples differ"
+    assert np.array_equal(it < -1.5, ref_it < -1.5), label + ": interior/exterior class differs"
+    if ref_en is not None:
+        mism = np.nonzero(en != ref_en)[0]
+        assert mism.size == 0, "%s: escape iteration differs at %d samples, first %s" % (label, mism.size, [(int(i), int(en[i]), int(ref_en[i])) for i in mism[:5]])
+    np.testing.assert_allclose(it, ref_it, rtol=RTOL, atol=0, err_msg=label)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_exact_matches_oracle(backend, name):
+    c = CASES[name]
+    it, nr, en, st = gpu_render(backend, c)
+    oit, onr, oen, ost = oracle.render(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"])
+    assert_same(it, en, oit, oen, name)
+    if c["coloring_method"] & 64:
+        np.testing.assert_allclose(nr, onr, rtol=RTOL, atol=0)
+    assert st["kernel_launches"] > 0 and st["samples"] > 0
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_exact_matches_reference_fixture(backend, name):
+    c = CASES[name]
+    it, nr, en, _ = gpu_render(backend, c)
+    ref_it, ref_nr = load_fixture(name, c)
+    assert_same(it, en, ref_it, None, name)
+    if ref_nr is not None:
+        np.testing.assert_allclose(nr, ref_nr, rtol=RTOL, atol=0)
+
+
+def test_repeat_is_deterministic(backend):
+    c = CASES["flake"]
+    a = gpu_render(backend, c)[0]
+    b = gpu_render(backend, c)[0]
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_device_outputs(backend):
+    torch = pytest.importorskip("torch")
+    c = CASES["minibrot875"]
+    n = c["width"] * c["height"]
+    it = torch.empty(n, dtype=torch.float32, device="cuda")
+    en = torch.empty(n, dtype=torch.int32, device="cuda")
+    req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], bailout=c["bailout"], iterations=it, escape_iteration=en)
+    assert backend.compute_status(req) == mbx.OK, backend.last_error()
+    host_it, _, host_en, _ = gpu_render(backend, c)
+    assert np.array_equal(it.cpu().numpy().view(np.uint32), host_it.view(np.uint32))
+    assert np.array_equal(en.cpu().numpy(), host_en)
+
+
+def test_invalid_requests_rejected(backend):
+    c = CASES["c1"]
+    for bad in (dict(sub=2), dict(width=1), dict(max_iterations=0), dict(coloring_method=8), dict(row_base=5)):
+        kw = dict(sub=1)
+        kw.update(bad)
+        req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], kw.pop("width", 16), 9, kw.pop("max_iterations", 100), **kw)
+        assert backend.compute_status(req) == mbx.E_INVALID
+    req = mbx.ComputeRequest("x", "0", "100", 16, 9, 100)
+    assert backend.compute_status(req) == mbx.E_INVALID
+
+
+def test_strip_render_matches_full_frame(backend):
+    """Strip export (full_height/row_base, mp.cpp:1399-1424) reproduces the
+    full frame row for row, like the reference's MANDEL_STRIPS check."""
+    c = dict(CASES["shallow"])
+    full = gpu_render(backend, c)[0].reshape(c["height"], c["width"])
+    sh = 32
+    for base in range(0, c["height"], sh):
+        h = min(sh, c["height"] - base)
+        req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], h, c["max_iterations"], bailout=c["bailout"], full_height=c["height"], row_base=base)
+        assert backend.compute_status(req) == mbx.OK
+        np.testing.assert_allclose(req.iterations.reshape(h, c["width"]), full[base : base + h], rtol=RTOL)

@@ -1,0 +1,59 @@
+"""Host-side arithmetic the device shares: the floatexp frexp/ldexp, the
+restated libgcc complex division used for series-approximation seeding, and the
+replica of glibc's rand() sequence. Compiled and checked against the C library
+of the machine running the tests."""
+import os
+import subprocess
+import tempfile
+
+from conftest import PKG
+
+PROGRAM = r"""
+#include "floatexp.h"
+#include "engine.h"
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+using namespace mbx;
+int main() {
+    std::mt19937_64 g(11);
+    std::uniform_real_distribution<double> u(-1, 1);
+    std::uniform_int_distribution<int> ue(-1080, 1080), uk(-2200, 2200);
+    long bad = 0;
+    for (long i = 0; i < 3000000; ++i) {
+        double x = std::ldexp(u(g), ue(g));
+        int k = uk(g);
+        if (dbits(std::ldexp(x, k)) != dbits(xldexp(x, k))) ++bad;
+        int e1, e2;
+        double f1 = std::frexp(x, &e1), f2 = xfrexp(x, &e2);
+        if (dbits(f1) != dbits(f2) || (x != 0 && e1 != e2)) ++bad;
+        double a = std::ldexp(u(g), ue(g) / 4), b = std::ldexp(u(g), ue(g) / 4), c = std::ldexp(u(g), ue(g) / 4), d = std::ldexp(u(g), ue(g) / 4);
+        std::complex<double> z(a, b), w(c, d);
+        z /= w;
+        C2 q = c_div(c2(a, b), c2(c, d));
+        double zr = z.real(), zi = z.imag();
+        if (std::isfinite(zr) && std::isfinite(zi) && (dbits(zr) != dbits(q.re) || dbits(zi) != dbits(q.im))) ++bad;
+    }
+    LibcRand r;
+    r.seed(1);
+    srand(1);
+    for (int i = 0; i < 100000; ++i)
+        if (r.next() != rand()) { ++bad; break; }
+    printf("%ld\n", bad);
+    return bad != 0;
+}
+"""
+
+
+def test_floatexp_complex_and_rand_match_libc():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.cpp")
+        exe = os.path.join(d, "t")
+        open(src, "w").write(PROGRAM)
+        csrc = os.path.join(PKG, "csrc")
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + csrc, "-I/usr/local/cuda/include", src, "-o", exe]
+        subprocess.check_call(cmd)
+        out = subprocess.run([exe], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
