@@ -58,6 +58,8 @@ typedef struct {
     float* normal;             /* optional: DE-overlay distance (MBX_DE_OVERLAY), else NULL */
     int32_t* escape_iteration; /* optional: escape iteration N per sample, -1 interior, -10 empty */
     volatile float* progress;  /* optional: 0..1 progress, written between passes */
+    int reuse_reference;       /* 1: reuse the previous frame's reference orbit and BLA table when the view,
+                                  size, iteration and coloring parameters are unchanged (zoom-sequence reuse) */
 } mbx_request;
 
 typedef struct {
@@ -69,6 +71,9 @@ typedef struct {
     long long gmp_pixels;           /* samples recomputed in arbitrary precision (mp.cpp:2173-2183) */
     long long samples;              /* samples computed */
     int passes, references, method, used_floatexp, period, reference_length, kernel_launches, interior;
+    double pass_gpu_ms;             /* CUDA-event time of the delta-pass kernels on the context's stream */
+    int reused_reference;           /* 1 when the cached reference was reused */
+    long long rebases;              /* rebases taken (mixed form) */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns
@@ -89,6 +94,20 @@ const char* mbx_info_name(const mbx_context* ctx);
 const char* mbx_info_detail(const mbx_context* ctx);
 const char* mbx_last_error(const mbx_context* ctx);
 int mbx_abi_version(void);
+
+/* Host-only nucleus search (no context, no GPU): findNucleus for the disk
+ * (centre, radius) — ball-arithmetic period up to max_period, then Newton
+ * refinement (src/engine/mandel_perturbation.cpp:116-223, 1072-1107) — with
+ * the minibrot size estimate of nucleusSizeMag (mp.cpp:1195-1219) returned as
+ * log10. Writes the nucleus as decimal strings (buf_len bytes each). Returns
+ * the period, 0 when the disk holds no nucleus, or a negative MBX_E_* code. */
+/* Diagnostic: measured issue rate of dependent-free FMA chains on the context's
+ * device, in TFLOP/s (an FMA counts as 2); fp64 = 1 for double, 0 for float.
+ * The roofline denominators of the delta loops (FP64 / FP32 pipes). */
+int mbx_measure_fma_peak(mbx_context* ctx, int fp64, double* tflops);
+
+int mbx_find_nucleus(const char* center_re, const char* center_im, const char* radius, int max_period, int precision_bits,
+                     char* nucleus_re, char* nucleus_im, int buf_len, double* size_log10);
 
 #ifdef __cplusplus
 }

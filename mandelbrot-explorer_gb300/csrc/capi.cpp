@@ -104,4 +104,25 @@ const char* mbx_info_name(const mbx_context* c) { return c ? c->name.c_str() : "
 const char* mbx_info_detail(const mbx_context* c) { return c ? c->detail.c_str() : ""; }
 const char* mbx_last_error(const mbx_context* c) { return c ? c->last_error.c_str() : ""; }
 
+int mbx_measure_fma_peak(mbx_context* c, int fp64, double* tflops) {
+    if (!c || !tflops) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    return c->engine->measure_fma_peak(fp64, tflops);
+}
+
+int mbx_find_nucleus(const char* center_re, const char* center_im, const char* radius, int max_period, int precision_bits, char* nucleus_re, char* nucleus_im, int buf_len, double* size_log10) {
+    if (!center_re || !center_im || !radius || !nucleus_re || !nucleus_im || buf_len < 8 || max_period < 1 || precision_bits < 64) return MBX_E_INVALID;
+    std::lock_guard<std::mutex> g(g_gmp_mutex);
+    std::string a, b;
+    int p = mbx::find_nucleus_disk(center_re, center_im, radius, max_period, precision_bits, a, b, size_log10);
+    if (p < 0) return MBX_E_INVALID;
+    if (p > 0 && ((int)a.size() >= buf_len || (int)b.size() >= buf_len)) return MBX_E_NOMEM;
+    if (p > 0) {
+        memcpy(nucleus_re, a.c_str(), a.size() + 1);
+        memcpy(nucleus_im, b.c_str(), b.size() + 1);
+    }
+    return p;
+}
+
 } // extern "C"

@@ -243,6 +243,7 @@ int Engine::init(std::string& err) {
     snprintf(devname_, sizeof(devname_), "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor, nsm_);
     if (cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess) return -1;
     if (cudaMalloc(&dctr_, sizeof(Counters)) != cudaSuccess) return -1;
+    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess) return -1;
     if (cudaHostAlloc(&hctr_, sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) return -1;
     if (cudaHostAlloc((void**)&hcancel_, sizeof(int), cudaHostAllocMapped) != cudaSuccess) return -1;
     *hcancel_ = 0;
@@ -254,9 +255,11 @@ void Engine::release_device() {
     if (st_) cudaStreamSynchronize(st_);
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
-                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p})
+                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dr2e_.p})
         if (p) cudaFree(p);
     if (dctr_) cudaFree(dctr_);
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
     if (hctr_) cudaFreeHost(hctr_);
     if (hcancel_) cudaFreeHost((void*)hcancel_);
     if (st_) cudaStreamDestroy(st_);
@@ -277,20 +280,6 @@ void Engine::reset_cancel() {
     }
 }
 
-template <typename T>
-bool Engine::ensure(DevBuf<T>& b, size_t n) {
-    if (n <= b.cap) return true;
-    if (b.p) cudaFree(b.p);
-    b.p = nullptr;
-    b.cap = 0;
-    size_t want = std::max<size_t>(n, 1);
-    if (cudaMalloc(&b.p, want * sizeof(T)) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    b.cap = want;
-    return true;
-}
 
 void Engine::set_precision(int p) { // mp.cpp:2030-2045
     if (!mpf_ready_) {
@@ -1053,6 +1042,7 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     const int threads = 128;
     const double t0 = now_ms();
     cudaError_t e;
+    cudaEventRecord(ev0_, st_);
     if (use_floatexp_ && mode_ == MBX_PRECISION_MIXED) {
         e = run_mixed_pass(f);
     } else if (use_floatexp_) {
@@ -1102,10 +1092,16 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     }
     ++stats_.kernel_launches;
     if (e != cudaSuccess) return fail_cuda("delta pass launch", e);
+    cudaEventRecord(ev1_, st_);
     cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("delta pass", e);
+    {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) stats_.pass_gpu_ms += ms;
+    }
+    stats_.rebases += (long long)hctr_->rebases;
     if (cancel_.load()) return MBX_E_CANCELLED;
     stats_.steps += (long long)hctr_->steps;
     stats_.bla_applies += (long long)hctr_->bla_applies;
@@ -1164,6 +1160,10 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
                 memcpy(new_ref, a, sizeof(a));
             }
         }
+    }
+    if (use_floatexp_ && !pending.empty()) {
+        err_ = "floatexp pass left samples unfinished";
+        return MBX_E_CUDA;
     }
     if (keys) keys->swap(pending);
     else if (!pending.empty()) {
@@ -1268,6 +1268,13 @@ int Engine::compute_frame(const mbx_request& r) {
     }
     mpf_set_default_prec((mp_bitcnt_t)prec);
     set_precision(prec);
+    {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "|%d|%d|%d|%d|%d|%d|%d|%d|%.17g|%d|", prec, W_, H_, full_h, row_base, SUB_, MXIT_, cm_, (double)escf_, mode_);
+        frame_key_ = std::string(r.center_re) + "|" + r.center_im + "|" + r.scale + buf;
+        reuse_ = r.reuse_reference && cache_.valid && cache_.key == frame_key_;
+        if (!reuse_) cache_.valid = false;
+    }
     MpfTemp cre, cim, msc;
     if (mpf_set_str(cre, r.center_re, 10) != 0 || mpf_set_str(cim, r.center_im, 10) != 0 || mpf_set_str(msc, r.scale, 10) != 0 || mpf_sgn(msc) <= 0) {
         err_ = "unparsable centre or scale";
@@ -1352,24 +1359,33 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     fe_cutoff_sensitive_ = false;
     dxfe_ = mpf_fe(dx_);
     dyfe_ = mpf_fe(dy_);
-    int ref_it = reference_for_frame();
-    if (cancel_.load()) return MBX_E_CANCELLED;
-    stats_.reference_length = ref_period_ > 0 ? ref_period_ : ref_it;
-    if (ref_subpixel_) use_bla_ = false;
-    int rc = upload_reference(ref_it);
-    if (rc != MBX_OK) return rc;
-    if (use_bla_) {
-        rc = build_bla(ref_period_ > 0 ? ref_period_ : ref_it);
+    int ref_it = 0;
+    int rc = MBX_OK;
+    refs_built_in_frame_ = 0;
+    if (reuse_ && restore_cache(&ref_it)) {
+        stats_.reused_reference = 1;
+    } else {
+        ref_it = reference_for_frame();
+        if (cancel_.load()) return MBX_E_CANCELLED;
+        stats_.reference_length = ref_period_ > 0 ? ref_period_ : ref_it;
+        if (ref_subpixel_) use_bla_ = false;
+        rc = upload_reference(ref_it);
         if (rc != MBX_OK) return rc;
+        if (use_bla_) {
+            rc = build_bla(ref_period_ > 0 ? ref_period_ : ref_it);
+            if (rc != MBX_OK) return rc;
+        }
+        if (!use_floatexp_) {
+            rc = build_dc_tables();
+            if (rc != MBX_OK) return rc;
+        }
+        if (mode_ == MBX_PRECISION_MIXED && use_floatexp_) {
+            rc = prepare_mixed();
+            if (rc != MBX_OK) return rc;
+        }
+        save_cache(ref_it);
     }
-    if (!use_floatexp_) {
-        rc = build_dc_tables();
-        if (rc != MBX_OK) return rc;
-    }
-    if (mode_ == MBX_PRECISION_MIXED && use_floatexp_) {
-        rc = prepare_mixed();
-        if (rc != MBX_OK) return rc;
-    }
+    refs_built_in_frame_ = 0;
     rc = flush_ref_value();
     if (rc != MBX_OK) return rc;
     if (progress) *progress = 0.08f;
@@ -1423,6 +1439,7 @@ int Engine::glitch_loop(std::vector<uint64_t>& pending, int& ref_it, bool have, 
         if (!have || it == pending.end() || *it != want) it = pending.begin() + (rng_.next() % pending.size());
         key_unpack(*it, pick);
         pending.erase(it);
+        cache_.valid = false; // the frame's reference changes
         ref_it = build_reference(pick, false);
         if (cancel_.load()) return MBX_E_CANCELLED;
         int rc = upload_reference(ref_it);
@@ -1496,6 +1513,7 @@ int Engine::supersample(int ref_it) {
         if (!have || it == samples.end() || *it != want) it = samples.begin() + (rng_.next() % samples.size());
         key_unpack(*it, pick);
         samples.erase(it);
+        cache_.valid = false;
         ref_it = build_reference(pick, false);
         rc = upload_reference(ref_it);
         if (rc != MBX_OK) break;
@@ -1584,6 +1602,146 @@ int Engine::shallow_samples(const std::vector<uint64_t>& samples) {
     stats_.interior += (int)hctr_->interior;
     stats_.samples += n;
     return MBX_OK;
+}
+
+} // namespace mbx
+
+namespace mbx {
+
+// findNucleus for an arbitrary disk (mp.cpp:1072-1107) plus the minibrot size
+// estimate of nucleusSizeMag (mp.cpp:1195-1219) evaluated on the nucleus orbit.
+int find_nucleus_disk(const char* cre, const char* cim, const char* radius, int maxp, int prec, std::string& nre, std::string& nim, double* size_log10) {
+    mpf_set_default_prec((mp_bitcnt_t)prec);
+    MpfTemp cr(prec), ci(prec), r(prec), nr(prec), ni(prec), dr(prec), di(prec), dist(prec);
+    if (mpf_set_str(cr, cre, 10) || mpf_set_str(ci, cim, 10) || mpf_set_str(r, radius, 10)) return -1;
+    int p = ball_period(cr, ci, r, maxp, prec, nullptr);
+    if (p <= 0) return 0;
+    mpf_set(nr, cr);
+    mpf_set(ni, ci);
+    if (!newton_nucleus(nr, ni, p, prec, 200)) return 0;
+    mpf_sub(dr, nr, cr);
+    mpf_sub(di, ni, ci);
+    mpf_mul(dr, dr, dr);
+    mpf_mul(di, di, di);
+    mpf_add(dist, dr, di);
+    mpf_sqrt(dist, dist);
+    if (mpf_cmp(dist, r) > 0) return 0;
+    // Size: l = prod 2 z_k, b = 1 + sum 1/l_k over k = 1..p-1, |size| = 1/(|b| |l|^2).
+    MpfTemp zr(prec), zi(prec), s1(prec), s2(prec), s3(prec);
+    mpf_set_ui(zr, 0);
+    mpf_set_ui(zi, 0);
+    FE lr = fe_make(1.0, 0), li = fe_make(0.0, 0), br = fe_make(1.0, 0), bi = fe_make(0.0, 0);
+    for (int k = 1; k < p; ++k) {
+        sqadd(zr, zi, nr, ni, s1, s2, s3);
+        FE xr = mpf_fe(zr), xi = mpf_fe(zi);
+        FE tr = fe_scale2(fe_sub(fe_mul(xr, lr), fe_mul(xi, li)), 1);
+        FE ti = fe_scale2(fe_add(fe_mul(xr, li), fe_mul(xi, lr)), 1);
+        lr = tr;
+        li = ti;
+        FE l2 = fe_add(fe_mul(lr, lr), fe_mul(li, li));
+        if (l2.m == 0.0) continue;
+        br = fe_add(br, fe_div(lr, l2));
+        bi = fe_sub(bi, fe_div(li, l2));
+    }
+    FE lmag = fe_sqrt(fe_add(fe_mul(lr, lr), fe_mul(li, li)));
+    FE bmag = fe_sqrt(fe_add(fe_mul(br, br), fe_mul(bi, bi)));
+    FE denom = fe_mul(bmag, fe_mul(lmag, lmag));
+    if (size_log10) *size_log10 = denom.m == 0.0 ? 0.0 : -(std::log10(std::fabs(denom.m)) + (double)denom.e * std::log10(2.0));
+    auto to_str = [&](mpf_ptr v) {
+        mp_exp_t e;
+        char* d = mpf_get_str(nullptr, &e, 10, 0, v);
+        std::string s(d);
+        free(d);
+        bool neg = !s.empty() && s[0] == '-';
+        if (neg) s.erase(0, 1);
+        std::string out = neg ? "-0." : "0.";
+        if (e < 0) out += std::string((size_t)(-e), '0');
+        else if (e > 0) {
+            out = (neg ? "-" : "") + s.substr(0, std::min<size_t>(s.size(), (size_t)e));
+            if ((size_t)e > s.size()) out += std::string((size_t)e - s.size(), '0');
+            s = s.size() > (size_t)e ? s.substr((size_t)e) : "";
+            out += ".";
+        }
+        out += s.empty() ? "0" : s;
+        return out;
+    };
+    nre = to_str(nr);
+    nim = to_str(ni);
+    return p;
+}
+
+} // namespace mbx
+
+namespace mbx {
+
+void Engine::save_cache(int ref_it) {
+    RefCache& c = cache_;
+    c.key = frame_key_;
+    c.use_floatexp = use_floatexp_;
+    c.use_bla = use_bla_;
+    c.ref_subpixel = ref_subpixel_;
+    c.ref_virtual = ref_virtual_;
+    c.fe_cutoff_sensitive = fe_cutoff_sensitive_;
+    c.ref_value_pending = ref_value_pending_;
+    c.ref_period = ref_period_;
+    memcpy(c.ref, ref_, sizeof(ref_));
+    c.orbit_len = orbit_len_;
+    c.sa_order = sa_order_;
+    c.sa_it = sa_it_;
+    c.ref_it = ref_it;
+    c.dc_xoff = dc_xoff_;
+    c.dc_yoff = dc_yoff_;
+    c.reference_length = stats_.reference_length;
+    c.ref_x = ref_x_;
+    c.ref_y = ref_y_;
+    c.ref_frac_re = ref_frac_re_;
+    c.ref_frac_im = ref_frac_im_;
+    for (int q = 0; q < kSaTerms; ++q) {
+        c.A[q] = sa_A_[q];
+        c.B[q] = sa_B_[q];
+    }
+    c.delta = sa_delta_;
+    c.bla = bla_;
+    c.dxfe = dxfe_;
+    c.dyfe = dyfe_;
+    c.ref_value = ref_value_;
+    c.ref_n = ref_n_;
+    c.valid = true;
+}
+
+bool Engine::restore_cache(int* ref_it) {
+    const RefCache& c = cache_;
+    if (!c.valid) return false;
+    use_floatexp_ = c.use_floatexp;
+    use_bla_ = c.use_bla;
+    ref_subpixel_ = c.ref_subpixel;
+    ref_virtual_ = c.ref_virtual;
+    fe_cutoff_sensitive_ = c.fe_cutoff_sensitive;
+    ref_value_pending_ = c.ref_value_pending;
+    ref_period_ = c.ref_period;
+    memcpy(ref_, c.ref, sizeof(ref_));
+    orbit_len_ = c.orbit_len;
+    sa_order_ = c.sa_order;
+    sa_it_ = c.sa_it;
+    dc_xoff_ = c.dc_xoff;
+    dc_yoff_ = c.dc_yoff;
+    stats_.reference_length = c.reference_length;
+    ref_x_ = c.ref_x;
+    ref_y_ = c.ref_y;
+    ref_frac_re_ = c.ref_frac_re;
+    ref_frac_im_ = c.ref_frac_im;
+    for (int q = 0; q < kSaTerms; ++q) {
+        sa_A_[q] = c.A[q];
+        sa_B_[q] = c.B[q];
+    }
+    sa_delta_ = c.delta;
+    bla_ = c.bla;
+    dxfe_ = c.dxfe;
+    dyfe_ = c.dyfe;
+    ref_value_ = c.ref_value;
+    ref_n_ = c.ref_n;
+    *ref_it = c.ref_it;
+    return true;
 }
 
 } // namespace mbx

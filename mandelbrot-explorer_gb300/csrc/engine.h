@@ -67,6 +67,7 @@ struct DevBuf {
 
 int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_t prec, const std::atomic<bool>* cancel);
 bool newton_nucleus(mpf_ptr cr, mpf_ptr ci, int period, mp_bitcnt_t prec, int maxit);
+int find_nucleus_disk(const char* cre, const char* cim, const char* radius, int maxp, int prec, std::string& nre, std::string& nim, double* size_log10);
 
 class Engine {
   public:
@@ -189,14 +190,59 @@ class Engine {
     DevBuf<uint64_t> dkeys_;
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
+    DevBuf<int16_t> dr2e_;
+
+    // mixed-pass launch shape (set by the autotuner / defaults)
+    int mixed_threads_ = 256;
+    int mixed_blocks_per_sm_ = 2;
+    int smem_orbit_limit_ = 200 * 1024;
     float* out_iter_ = nullptr;
     float* out_norm_ = nullptr;
     int32_t* out_n_ = nullptr;
 
+    // reference cache (mbx_request.reuse_reference)
+    struct RefCache {
+        bool valid = false;
+        std::string key;
+        bool use_floatexp, use_bla, ref_subpixel, ref_virtual, fe_cutoff_sensitive, ref_value_pending;
+        int ref_period, ref[4], orbit_len, sa_order, sa_it, ref_it, dc_xoff, dc_yoff, reference_length;
+        double ref_x, ref_y, ref_frac_re, ref_frac_im;
+        C2 A[kSaTerms], B[kSaTerms], delta;
+        BlaView bla;
+        FE dxfe, dyfe;
+        float ref_value;
+        int32_t ref_n;
+    } cache_;
+    std::string frame_key_;
+    bool reuse_ = false;
+    int refs_built_in_frame_ = 0;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    void save_cache(int ref_it);
+    bool restore_cache(int* ref_it);
+
+  public:
+    int measure_fma_peak(int fp64, double* tflops);
+
+  private:
     // pass readback
     std::vector<uint8_t> hdone_, hgmp_;
     std::vector<double> hglitch_;
     std::vector<uint64_t> grid_pending_;
 };
+
+template <typename T>
+bool Engine::ensure(DevBuf<T>& b, size_t n) {
+    if (n <= b.cap) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = n > 0 ? n : 1;
+    if (cudaMalloc(&b.p, want * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    b.cap = want;
+    return true;
+}
 
 } // namespace mbx

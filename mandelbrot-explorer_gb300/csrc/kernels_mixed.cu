@@ -1,7 +1,563 @@
-// Mixed-precision pass (placeholder until the FP32 floatexp kernel lands).
+// Mixed-precision floatexp pass. The bulk delta iteration runs in FP32 on a
+// rescaled delta dz = S * w, with S an FP32-mantissa floatexp (float m, int e)
+// and w an O(1) float2; the reference orbit is read as float2 from shared
+// memory (staged once per block by a TMA bulk copy) or from L1/L2 when it does
+// not fit. On GB300 one FP64 instruction costs as much issue time as ~60 FP32
+// ones, so FP64 (and FP64-mantissa floatexp) is used only on rare events:
+//   * BLA skips: coefficients and validity radii come from the FP64 table;
+//     candidates are screened on integer exponents, decided and applied in FP64;
+//   * rebasing near |Z + dz| ~ |dz|: screened in FP32, decided in FP64-floatexp;
+//   * escape: screened in FP32 with a relative margin, decided and the smooth
+//     value computed from an FP64 reconstruction of z;
+//   * interior detection: FP32 screen, FP64 at close returns and saves;
+//   * steps where the orbit is below FP32's range (exact floatexp step).
+// Semantics follow the reference's rescaled loop (mp.cpp:3287-3618); results
+// are validated against the arbitrary-precision oracle, not bit-compared.
+#include <cuda_runtime.h>
+
 #include "engine.h"
 
 namespace mbx {
-cudaError_t Engine::run_mixed_pass(const DeviceFrame&) { return cudaErrorNotSupported; }
-int Engine::prepare_mixed() { return MBX_OK; }
+
+namespace {
+
+constexpr double kLn2m = 0x1.62e42fefa39efp-1;
+
+__device__ __forceinline__ bool mcancelled(const DeviceFrame& f) { return f.cancel && *f.cancel; }
+
+// ---- FP32-mantissa floatexp: m in [0.5,1) (or 0), e int -------------------
+struct F32E {
+    float m;
+    int e;
+};
+__device__ __forceinline__ F32E f32e_norm(float m, int e) {
+    if (m == 0.0f) return F32E{0.0f, 0};
+    unsigned b = __float_as_uint(m);
+    int ex = (int)((b >> 23) & 0xff);
+    if (ex == 0) { // subnormal mantissa: scale up exactly
+        m *= 16777216.0f;
+        b = __float_as_uint(m);
+        ex = (int)((b >> 23) & 0xff) - 24;
+    }
+    return F32E{__uint_as_float((b & 0x807fffffu) | (126u << 23)), e + ex - 126};
+}
+__device__ __forceinline__ F32E f32e_mulf(F32E a, float b) { return f32e_norm(a.m * b, a.e); }
+// a * 2^k as float, flushing below FP32's normal range to zero.
+__device__ __forceinline__ float ldexpf_ftz(float a, int k) {
+    if (a == 0.0f) return 0.0f;
+    unsigned b = __float_as_uint(a);
+    int ex = (int)((b >> 23) & 0xff) + k;
+    if (ex <= 0) return 0.0f;
+    if (ex >= 255) return __uint_as_float((b & 0x80000000u) | 0x7f7fffffu);
+    return __uint_as_float((b & 0x807fffffu) | ((unsigned)ex << 23));
+}
+__device__ __forceinline__ float f32e_to_float(F32E a) { return ldexpf_ftz(a.m, a.e); }
+__device__ __forceinline__ F32E f32e_from_fe(FE a) {
+    if (a.m == 0.0) return F32E{0.0f, 0};
+    return f32e_norm((float)a.m, (int)a.e);
+}
+__device__ __forceinline__ FE fe_from_f32e(F32E a) { return a.m == 0.0f ? fe_make(0.0, 0) : fe_make((double)a.m, (int64_t)a.e); }
+// x / S for x, S in F32E, as float.
+__device__ __forceinline__ float f32e_ratio(F32E x, F32E s) {
+    if (x.m == 0.0f) return 0.0f;
+    return ldexpf_ftz(__fdividef(x.m, s.m), x.e - s.e);
+}
+__device__ __forceinline__ int float_exp(float x) { return (int)((__float_as_uint(x) >> 23) & 0xff) - 127; }
+
+// Exact floatexp step for orbit entries below FP32's range (mp.cpp:2794-2835).
+__device__ void exact_step(FE Xr, FE Xi, FE dcr, FE dci, FE& S, double& wr, double& wi) {
+    const double sm = S.m, sm2 = sm * sm;
+    const int64_t se = S.e;
+    const int64_t NONE = (int64_t)0x8000000000000000ll;
+    int64_t e = NONE;
+    const bool has_w = wr != 0.0 || wi != 0.0;
+    if (has_w && Xr.m != 0.0) e = max(e, Xr.e + se);
+    if (has_w && Xi.m != 0.0) e = max(e, Xi.e + se);
+    if (has_w) e = max(e, se + se);
+    if (dcr.m != 0.0) e = max(e, dcr.e);
+    if (dci.m != 0.0) e = max(e, dci.e);
+    if (e == NONE) {
+        S = fe_make(1.0, 0);
+        wr = wi = 0.0;
+        return;
+    }
+    auto align = [e](double m, int64_t te) -> double {
+        int64_t d = te - e;
+        if (m == 0.0 || d < -54) return 0.0;
+        return m * pow2i((int)d);
+    };
+    const double xs_r = align(Xr.m * sm, Xr.e + se);
+    const double xs_i = align(Xi.m * sm, Xi.e + se);
+    const double s2 = align(sm2, se + se);
+    const double cr = align(dcr.m, dcr.e);
+    const double ci = align(dci.m, dci.e);
+    const double nr = 2.0 * (xs_r * wr - xs_i * wi) + s2 * (wr * wr - wi * wi) + cr;
+    const double ni = 2.0 * (xs_r * wi + xs_i * wr) + 2.0 * s2 * wr * wi + ci;
+    const double mag = sqrt(nr * nr + ni * ni);
+    if (mag == 0.0) {
+        S = fe_make(1.0, 0);
+        wr = wi = 0.0;
+        return;
+    }
+    S = fe_renorm(mag, e);
+    wr = nr / mag;
+    wi = ni / mag;
+}
+
+struct MixedState {
+    F32E S;        // delta scale
+    float wr, wi;  // delta unit
+    float s;       // S as float (0 below FP32's range)
+    float dr, di;  // dc / S
+    F32E dcr, dci; // dc
+};
+
+__device__ __forceinline__ void refresh(MixedState& st) {
+    st.s = f32e_to_float(st.S);
+    st.dr = f32e_ratio(st.dcr, st.S);
+    st.di = f32e_ratio(st.dci, st.S);
+}
+
+// BLA skip (mp.cpp:2883-2970 semantics): levels screened on integer exponents
+// of |dz|^2 against the precomputed exponents of r2; decided and applied in FP64.
+__device__ int mixed_bla(const BlaView& b, const int16_t* r2e, const double2* Z, bool periodic, int s, MixedState& st, FE dcr, FE dci, double ESC2, int mx_ref_it) {
+    int maxp = b.nlev - 1;
+    int startp = (s == 1) ? maxp : __ffs(s - 1) - 1;
+    if (startp > maxp) startp = maxp;
+    if (startp < b.minlevel) return 0;
+    const float wm2 = st.wr * st.wr + st.wi * st.wi;
+    if (wm2 == 0.0f) return 0;
+    const int edz2 = 2 * st.S.e + float_exp(wm2) + 1; // |dz|^2 < 2^edz2
+    for (int p = startp; p >= b.minlevel; --p) {
+        int i = (s - 1) >> p;
+        if (i >= b.size[p]) continue;
+        const int er = r2e[b.off[p] + i];      // r2 >= 2^(er-1), or -32768 when r2 <= 0
+        if (er == -32768 || edz2 - 2 > er) continue; // clearly too large (or invalid)
+        const double r2 = b.r2[b.off[p] + i];
+        const double wr = st.wr, wi = st.wi;
+        const FE S = fe_from_f32e(st.S);
+        FE dz2 = fe_mul(fe_mul(S, S), fe_from(wr * wr + wi * wi));
+        if (!fe_abs_less(dz2, fe_from(r2))) continue;
+        int l = 1 << p;
+        int land = s + l;
+        if (land >= mx_ref_it - 1) continue;
+        const double dr = fe_to_double(fe_div(dcr, S)), di = fe_to_double(fe_div(dci, S));
+        double4 bc = b.ab[b.off[p] + i];
+        double nwr = (bc.x * wr - bc.y * wi) + (bc.z * dr - bc.w * di);
+        double nwi = (bc.x * wi + bc.y * wr) + (bc.z * di + bc.w * dr);
+        if (!(fabs(nwr) < 1e150 && fabs(nwi) < 1e150)) return 0;
+        double2 zl = Z[land];
+        double fr = zl.x + fe_to_double(fe_mul_d(S, nwr));
+        double fi = zl.y + fe_to_double(fe_mul_d(S, nwi));
+        if (fr * fr + fi * fi > ESC2) return 0;
+        double wm2d = nwr * nwr + nwi * nwi;
+        if (wm2d == 0.0) {
+            if (!periodic) return 0;
+            st.S = F32E{0.5f, 1};
+            st.wr = st.wi = 0.0f;
+        } else {
+            double wmag = sqrt(wm2d);
+            st.S = f32e_from_fe(fe_mul(S, fe_from(wmag)));
+            st.wr = (float)(nwr / wmag);
+            st.wi = (float)(nwi / wmag);
+        }
+        return l;
+    }
+    return 0;
+}
+
+// Stage the FP32 orbit into shared memory: bulk TMA copies (cp.async.bulk,
+// global -> shared) completing on one mbarrier; the wait is bounded.
+__device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned long long* mbar) {
+    const unsigned bytes = ((unsigned)entries * 8u + 15u) & ~15u;
+    const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+        const unsigned chunk = 1u << 15;
+        for (unsigned off = 0; off < bytes; off += chunk) {
+            unsigned n = bytes - off < chunk ? bytes - off : chunk;
+            unsigned dst = (unsigned)__cvta_generic_to_shared((char*)smem + off);
+            const char* src = (const char*)g + off;
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src), "r"(n), "r"(mb) : "memory");
+        }
+    }
+    __syncthreads();
+    unsigned done = 0;
+    for (int spin = 0; spin < (1 << 22) && !done; ++spin) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mb)
+            : "memory");
+    }
+    return done != 0;
+}
+
+__global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ unsigned long long mbar;
+    __shared__ int stage_ok;
+    const FrameGeom& g = p.g;
+    const float2* orb = p.Zf;
+    if (p.orbit_in_smem) {
+        float2* so = reinterpret_cast<float2*>(smem_raw);
+        bool ok = stage_orbit(so, p.Zf, p.smem_entries, &mbar);
+        if (threadIdx.x == 0) stage_ok = ok ? 1 : 0;
+        __syncthreads();
+        if (stage_ok) orb = so;
+        else if (threadIdx.x == 0) atomicAdd(&f.ctr->rescales, 1ull); // staging timed out: global reads
+        if (!stage_ok) return; // an in-flight copy must not land in a reused CTA slot; leave the work to other blocks
+    }
+    const double2* Zd = f.orbit.Z;
+    const FE2* Zfe = f.orbit.Zfe;
+    const int reflen = p.mx_ref_it + 1;
+    const int per = p.per;
+    const float ESC2f = (float)g.ESC2;
+    const float ESC2lo = ESC2f * 0.99999f;
+    const int blamask = (1 << f.bla.minlevel) - 1;
+    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0;
+    unsigned int n_int = 0;
+    for (;;) {
+        if (mcancelled(f)) break;
+        int i = (int)atomicAdd(&f.ctr->next, 1u);
+        if (i >= f.px.n) break;
+        int arr[4];
+        if (f.px.keys) {
+            key_unpack(f.px.keys[i], arr);
+        } else {
+            int cols = (f.px.grid_w + f.px.grid_step - 1) / f.px.grid_step;
+            int q = i;
+            if (f.px.skip_i >= 0) {
+                int sq = (f.px.skip_i / f.px.grid_step) * cols + f.px.skip_j / f.px.grid_step;
+                if (q >= sq) ++q;
+            }
+            arr[0] = (q / cols) * f.px.grid_step;
+            arr[1] = (q % cols) * f.px.grid_step;
+            arr[2] = arr[3] = 0;
+        }
+        const double px = arr[1] + (double)arr[3] / g.sub;
+        const double py = arr[0] + (double)arr[2] / g.sub;
+        const FE dcr = fe_mul_d(p.dxfe, px - p.ref_x);
+        const FE dci = fe_mul_d(p.dyfe, py - p.ref_y);
+        MixedState st;
+        st.dcr = f32e_from_fe(dcr);
+        st.dci = f32e_from_fe(dci);
+        {
+            FE S0 = fe_sqrt(fe_add(fe_mul(dcr, dcr), fe_mul(dci, dci)));
+            if (S0.m == 0.0) {
+                st.S = F32E{0.5f, 1};
+                st.wr = st.wi = 0.0f;
+            } else {
+                st.S = f32e_from_fe(S0);
+                st.wr = (float)fe_to_double(fe_div(dcr, S0));
+                st.wi = (float)fe_to_double(fe_div(dci, S0));
+            }
+        }
+        refresh(st);
+        int m = 1, iter = 1, rm = 0;
+        float2 Xc = make_float2(0.0f, 0.0f); // X_m (X_0 = 0)
+        Xc = orb[0];                          // m = 1 -> stored index 0
+        // Brent interior detector (mp.cpp:3533-3568), FP32 screen + FP64 confirm.
+        double zsr = 1e30, zsi = 1e30, conf_zr = 0, conf_zi = 0;
+        float zsr_f = 1e30f, zsi_f = 1e30f;
+        float conf_D2 = 0.0f;
+        int save_iter = 1, period_win = 1, conf_P = 0, conf_next = 0, conf_count = 0, conf_giveup = 0;
+        int outcome = 0, nesc = -1;
+        double zrad_d = 0.0;
+        int tick = 0;
+        while (iter < g.mxit) {
+            if (((++tick) & 8191) == 0 && mcancelled(f)) {
+                outcome = 4;
+                break;
+            }
+            if (f.bla.use && m >= 2 && ((rm - 1) & blamask) == 0) {
+                int skip = mixed_bla(f.bla, r2e, Zd, per > 0, rm, st, dcr, dci, g.ESC2, per ? per : reflen);
+                if (skip > 0) {
+                    ++n_bla;
+                    n_skip += skip;
+                    m += skip;
+                    iter += skip;
+                    rm += skip;
+                    if (per && rm >= per) rm -= per;
+                    refresh(st);
+                    Xc = orb[rm];
+                    zsr = zsi = 1e30;
+                    zsr_f = zsi_f = 1e30f;
+                    save_iter = iter;
+                    period_win = 1;
+                    conf_P = 0;
+                    conf_giveup = 0;
+                    continue;
+                }
+            }
+            ++n_steps;
+            // w' = (2 X_m + s w) w + d   (X_0 = 0 after a rebase)
+            const bool tiny = m != 0 && fabsf(Xc.x) < 1e-30f && fabsf(Xc.y) < 1e-30f && (Zfe[rm].re.m != 0.0 || Zfe[rm].im.m != 0.0);
+            if (!tiny) {
+                const float fR = 2.0f * Xc.x + st.s * st.wr;
+                const float fI = 2.0f * Xc.y + st.s * st.wi;
+                const float nwr = fR * st.wr - fI * st.wi + st.dr;
+                const float nwi = fR * st.wi + fI * st.wr + st.di;
+                st.wr = nwr;
+                st.wi = nwi;
+            } else {
+                double wr = st.wr, wi = st.wi;
+                FE S = fe_from_f32e(st.S);
+                exact_step(Zfe[rm].re, Zfe[rm].im, dcr, dci, S, wr, wi);
+                st.S = f32e_from_fe(S);
+                st.wr = (float)wr;
+                st.wi = (float)wi;
+                refresh(st);
+            }
+            ++m;
+            ++iter;
+            ++rm;
+            if (per && rm == per) rm = 0;
+            Xc = orb[rm];
+            const float zr = Xc.x + st.s * st.wr, zi = Xc.y + st.s * st.wi;
+            const float zrad = zr * zr + zi * zi;
+            if (zrad > ESC2lo) {
+                double2 Xd = Zd[rm];
+                double sd = fe_to_double(fe_from_f32e(st.S));
+                double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
+                zrad_d = zdr * zdr + zdi * zdi;
+                if (zrad_d > g.ESC2) {
+                    outcome = 1;
+                    nesc = iter;
+                    break;
+                }
+            }
+            if (p.use_interior) {
+                if (conf_P > 0) {
+                    conf_D2 *= 4.0f * zrad;
+                    if (conf_D2 > 1e18f) conf_D2 = 1e18f;
+                    if (iter >= conf_next) {
+                        double2 Xd = Zd[rm];
+                        double sd = fe_to_double(fe_from_f32e(st.S));
+                        double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
+                        double qr = zdr - conf_zr, qi = zdi - conf_zi;
+                        if (qr * qr + qi * qi < p.interior_eps2 * (zdr * zdr + zdi * zdi) && conf_D2 < 1.0f) {
+                            if (++conf_count >= p.interior_confirm) {
+                                outcome = 2;
+                                break;
+                            }
+                            conf_zr = zdr;
+                            conf_zi = zdi;
+                            conf_D2 = 1.0f;
+                            conf_next = iter + conf_P;
+                        } else {
+                            conf_P = 0;
+                            ++conf_giveup;
+                        }
+                    }
+                } else if ((iter & 15) == 0 && conf_giveup < 3) {
+                    // FP32 screen: |dz - saved|^2 far above eps^2 |z|^2 cannot be a return.
+                    const float qr = zr - zsr_f, qi = zi - zsi_f;
+                    const bool maybe = qr * qr + qi * qi < 1e-11f * zrad;
+                    const bool save = iter - save_iter >= period_win;
+                    if (maybe || save) {
+                        double2 Xd = Zd[rm];
+                        double sd = fe_to_double(fe_from_f32e(st.S));
+                        double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
+                        if (maybe) {
+                            double dqr = zdr - zsr, dqi = zdi - zsi;
+                            if (dqr * dqr + dqi * dqi < p.interior_eps2 * (zdr * zdr + zdi * zdi)) {
+                                conf_P = max(iter - save_iter, 1);
+                                conf_zr = zdr;
+                                conf_zi = zdi;
+                                conf_D2 = 1.0f;
+                                conf_next = iter + conf_P;
+                                conf_count = 0;
+                            }
+                        }
+                        if (save) {
+                            zsr = zdr;
+                            zsi = zdi;
+                            zsr_f = zr;
+                            zsi_f = zi;
+                            save_iter = iter;
+                            period_win += period_win;
+                        }
+                    }
+                }
+            }
+            // keep |w| ~ 1 (FP32-mantissa floatexp rescale)
+            const float wm2 = st.wr * st.wr + st.wi * st.wi;
+            if (wm2 > 1e16f || (wm2 < 1e-16f && wm2 > 0.0f)) {
+                const float wmag = sqrtf(wm2);
+                const float inv = 1.0f / wmag;
+                st.S = f32e_mulf(st.S, wmag);
+                st.wr *= inv;
+                st.wi *= inv;
+                refresh(st);
+            }
+            // Rebase: FP32 screen, FP64-floatexp decision (mp.cpp:3584-3615).
+            const float dzmag2 = st.s * st.s * (st.wr * st.wr + st.wi * st.wi);
+            if (zrad < 1e-8f || zrad < dzmag2 * 1.001f || (!per && m >= reflen)) {
+                const FE S = fe_from_f32e(st.S);
+                FE Xmr = Zfe[rm].re;
+                FE Xmi = Zfe[rm].im;
+                FE Swr = fe_mul_d(S, (double)st.wr), Swi = fe_mul_d(S, (double)st.wi);
+                FE zrfe = fe_add(Xmr, Swr), zife = fe_add(Xmi, Swi);
+                FE zradfe = fe_add(fe_mul(zrfe, zrfe), fe_mul(zife, zife));
+                FE dzfe = fe_add(fe_mul(Swr, Swr), fe_mul(Swi, Swi));
+                if ((!per && m >= reflen) || fe_abs_less(zradfe, dzfe)) {
+                    FE Snew = fe_sqrt(zradfe);
+                    if (Snew.m == 0.0) {
+                        st.wr = st.wi = 0.0f;
+                    } else {
+                        st.S = f32e_from_fe(Snew);
+                        st.wr = (float)fe_to_double(fe_div(zrfe, Snew));
+                        st.wi = (float)fe_to_double(fe_div(zife, Snew));
+                        refresh(st);
+                    }
+                    m = 0;
+                    rm = -1;
+                    Xc = make_float2(0.0f, 0.0f);
+                    ++n_rebase;
+                }
+            }
+        }
+        if (outcome == 4) break;
+        if (outcome == 0) outcome = 2;
+        const int idx = (arr[0] * g.sub + g.sub / 2 + arr[2]) * g.W * g.sub + (arr[1] * g.sub + g.sub / 2 + arr[3]);
+        if (outcome == 1) {
+            f.out.iter[idx] = (float)((double)nesc - log(log(zrad_d) / 2.0 / kLn2m) / kLn2m);
+            if (f.out.escN) f.out.escN[idx] = nesc;
+            n_eff += (unsigned long long)nesc;
+        } else {
+            f.out.iter[idx] = -2.0f;
+            if (f.out.escN) f.out.escN[idx] = -1;
+            n_eff += (unsigned long long)g.mxit;
+            ++n_int;
+        }
+        f.out.done[i] = 1;
+    }
+    atomicAdd(&f.ctr->steps, n_steps);
+    atomicAdd(&f.ctr->bla_applies, n_bla);
+    atomicAdd(&f.ctr->bla_skipped, n_skip);
+    atomicAdd(&f.ctr->effective_iters, n_eff);
+    atomicAdd(&f.ctr->rebases, n_rebase);
+    atomicAdd(&f.ctr->interior, n_int);
+}
+
+__global__ void k_orbit_to_float(const double2* Z, float2* Zf, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) Zf[i] = make_float2((float)Z[i].x, (float)Z[i].y);
+}
+
+// Exponent of each BLA radius^2 (r2 in [2^(e-1), 2^e)), -32768 for r2 <= 0.
+__global__ void k_bla_exponents(const double* r2, int16_t* e, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = r2[i];
+    if (!(v > 0.0)) {
+        e[i] = -32768;
+        return;
+    }
+    int ex;
+    (void)xfrexp(v, &ex);
+    e[i] = (int16_t)max(-32767, min(32767, ex));
+}
+
+__global__ void k_fma_probe_f32(float* out, int iters, float a, float b) {
+    float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = __fmaf_rn(x0, a, b); x1 = __fmaf_rn(x1, a, b); x2 = __fmaf_rn(x2, a, b); x3 = __fmaf_rn(x3, a, b);
+        x4 = __fmaf_rn(x4, a, b); x5 = __fmaf_rn(x5, a, b); x6 = __fmaf_rn(x6, a, b); x7 = __fmaf_rn(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+__global__ void k_fma_probe_f64(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = __fma_rn(x0, a, b); x1 = __fma_rn(x1, a, b); x2 = __fma_rn(x2, a, b); x3 = __fma_rn(x3, a, b);
+        x4 = __fma_rn(x4, a, b); x5 = __fma_rn(x5, a, b); x6 = __fma_rn(x6, a, b); x7 = __fma_rn(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+} // namespace
+
+int Engine::measure_fma_peak(int fp64, double* tflops) {
+    const int blocks = nsm_ * 8, threads = 256;
+    const int iters = fp64 ? 2000 : 40000;
+    void* buf = nullptr;
+    if (cudaMalloc(&buf, (size_t)blocks * threads * 8) != cudaSuccess) return MBX_E_NOMEM;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(ev0_, st_);
+        if (fp64) k_fma_probe_f64<<<blocks, threads, 0, st_>>>((double*)buf, iters, 0.999999, 1e-7);
+        else k_fma_probe_f32<<<blocks, threads, 0, st_>>>((float*)buf, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(ev1_, st_);
+        cudaError_t e = cudaEventSynchronize(ev1_);
+        if (e != cudaSuccess) {
+            cudaFree(buf);
+            return fail_cuda("fma probe", e);
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0_, ev1_);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaFree(buf);
+    *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (best * 1e-3) / 1e12;
+    return MBX_OK;
+}
+
+cudaError_t launch_mixed_pass(const DeviceFrame& f, const MixedParams& p, int blocks, int threads, size_t smem, cudaStream_t st) {
+    (void)f;
+    (void)p;
+    (void)blocks;
+    (void)threads;
+    (void)smem;
+    (void)st;
+    return cudaErrorNotSupported; // launched through Engine::run_mixed_pass (needs the exponent table)
+}
+
+int Engine::prepare_mixed() {
+    const int len = orbit_len_;
+    if (!ensure(dZf_, (size_t)len + 4)) return MBX_E_NOMEM;
+    k_orbit_to_float<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZf_.p, len);
+    ++stats_.kernel_launches;
+    if (bla_.use && bla_.nlev > 0) {
+        int n = bla_.off[bla_.nlev - 1] + bla_.size[bla_.nlev - 1];
+        if (!ensure(dr2e_, (size_t)n)) return MBX_E_NOMEM;
+        k_bla_exponents<<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dr2e_.p, n);
+        ++stats_.kernel_launches;
+    }
+    return cuda_ok("mixed preparation");
+}
+
+cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
+    MixedParams p;
+    p.g = geom();
+    p.dxfe = dxfe_;
+    p.dyfe = dyfe_;
+    p.ref_x = ref_x_;
+    p.ref_y = ref_y_;
+    p.per = ref_period_;
+    p.mx_ref_it = ref_period_ > 0 ? ref_period_ : orbit_len_ - 1;
+    p.use_interior = use_interior_ ? 1 : 0;
+    p.interior_eps2 = interior_eps2_;
+    p.interior_confirm = interior_confirm_;
+    p.Zf = dZf_.p;
+    p.Zsmall = nullptr;
+    const size_t bytes = ((size_t)orbit_len_ * 8 + 15) & ~(size_t)15;
+    p.orbit_in_smem = (bytes <= (size_t)smem_orbit_limit_) ? 1 : 0;
+    p.smem_entries = orbit_len_;
+    const int threads = mixed_threads_;
+    const int blocks = std::max(1, std::min((f.px.n + threads - 1) / threads, nsm_ * mixed_blocks_per_sm_));
+    const size_t smem = p.orbit_in_smem ? bytes : 0;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_mixed_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    DeviceFrame g = f;
+    if (!(bla_.use && dr2e_.p)) g.bla.use = 0;
+    k_mixed_pass<<<blocks, threads, smem, st_>>>(g, p, dr2e_.p);
+    return cudaGetLastError();
+}
+
 } // namespace mbx

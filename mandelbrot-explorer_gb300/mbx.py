@@ -60,6 +60,7 @@ class _Request(ctypes.Structure):
         ("normal", ctypes.c_void_p),
         ("escape_iteration", ctypes.c_void_p),
         ("progress", ctypes.c_void_p),
+        ("reuse_reference", ctypes.c_int),
     ]
 
 
@@ -84,6 +85,9 @@ class Stats(ctypes.Structure):
         ("reference_length", ctypes.c_int),
         ("kernel_launches", ctypes.c_int),
         ("interior", ctypes.c_int),
+        ("pass_gpu_ms", ctypes.c_double),
+        ("reused_reference", ctypes.c_int),
+        ("rebases", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -101,6 +105,8 @@ EXPORTS = (
     "mbx_info_detail",
     "mbx_last_error",
     "mbx_abi_version",
+    "mbx_find_nucleus",
+    "mbx_measure_fma_peak",
 )
 
 _lib = None
@@ -133,6 +139,10 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
             getattr(lib, fn).restype = ctypes.c_char_p
             getattr(lib, fn).argtypes = [ctypes.c_void_p]
         lib.mbx_abi_version.restype = ctypes.c_int
+        lib.mbx_measure_fma_peak.restype = ctypes.c_int
+        lib.mbx_measure_fma_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.mbx_find_nucleus.restype = ctypes.c_int
+        lib.mbx_find_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         if path is None:
             _lib = lib
         return lib
@@ -188,6 +198,7 @@ class ComputeRequest:
     escape_iteration: object = None
     want_escape_iteration: bool = True
     progress: Optional[ctypes.c_float] = None
+    reuse_reference: bool = False
 
     def sample_count(self) -> int:
         return self.width * self.height * self.sub * self.sub
@@ -277,12 +288,21 @@ class CudaComputeBackend:
             nr,
             en,
             ctypes.cast(ctypes.pointer(req.progress), ctypes.c_void_p) if req.progress is not None else None,
+            1 if req.reuse_reference else 0,
         )
         st = Stats()
         rc = self._lib.mbx_compute(self._ctx, ctypes.byref(r), ctypes.byref(st))
         self.last_stats = st
         self.last_status = rc
         return rc
+
+    def measure_fma_peak(self, fp64: bool) -> float:
+        """Measured FMA issue rate of the device in TFLOP/s (FMA = 2 flops)."""
+        v = ctypes.c_double(0.0)
+        rc = self._lib.mbx_measure_fma_peak(self._ctx, 1 if fp64 else 0, ctypes.byref(v))
+        if rc != OK:
+            raise RuntimeError("peak probe failed: " + self.last_error())
+        return v.value
 
     def compute(self, req: ComputeRequest) -> bool:
         """True on success, like IComputeBackend::compute."""
@@ -295,6 +315,21 @@ def create_compute_backend(requested: str = "cuda", device: int = 0) -> CudaComp
     if name not in ("cuda", "gpu", "gb300", "auto"):
         raise ValueError("unknown backend %r (this library provides only the CUDA backend)" % requested)
     return CudaComputeBackend(device)
+
+
+def find_nucleus(center_re: str, center_im: str, radius: str, max_period: int, precision_bits: int):
+    """Host-only nucleus search: returns (period, nucleus_re, nucleus_im, log10 size) or None."""
+    lib = load_library()
+    n = precision_bits // 3 + 64
+    a = ctypes.create_string_buffer(n)
+    b = ctypes.create_string_buffer(n)
+    sz = ctypes.c_double(0.0)
+    p = lib.mbx_find_nucleus(center_re.encode(), center_im.encode(), radius.encode(), max_period, precision_bits, a, b, n, ctypes.byref(sz))
+    if p < 0:
+        raise ValueError("mbx_find_nucleus failed (%d)" % p)
+    if p == 0:
+        return None
+    return p, a.value.decode(), b.value.decode(), sz.value
 
 
 def render(center_re, center_im, scale, width, height, max_iterations, **kw):

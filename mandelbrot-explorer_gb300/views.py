@@ -33,3 +33,63 @@ def c1_view(seed: int = 1):
     cre = extend_digits(C1_BASE_RE, 120, rng)
     cim = extend_digits(C1_BASE_IM, 120, rng)
     return {"center_re": cre, "center_im": cim, "scale": "2" + "0" * 30, "max_iterations": 50000, "bailout": 256.0}
+
+
+# ---------------------------------------------------------------------------
+# Deep frames: 1920x1080, maxiter 1e6, centred a seed-drawn 10^-(k+5) vector
+# away from the Newton-refined nucleus of a period-p component (p = 14164, in
+# [2000, 20000]) at half-widths 10^-300 and 10^-1000. The nucleus is stored in
+# views_data.json (regenerate with ``python views.py --regenerate``).
+import json
+import math
+import os
+from decimal import Decimal, getcontext
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA = os.path.join(HERE, "views_data.json")
+
+
+def nucleus():
+    with open(DATA) as f:
+        return json.load(f)
+
+
+def deep_view(k: int, seed: int = 2, width: int = 1920, height: int = 1080, max_iterations: int = 1_000_000, bailout: float = 256.0):
+    d = nucleus()
+    rng = np.random.RandomState(seed * 1000 + k)
+    ang = rng.uniform(0.0, 2.0 * math.pi)
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    off = Decimal(10) ** (-(k + 5))
+    cre = Decimal(d["nucleus_re"]) + off * Decimal(repr(math.cos(ang)))
+    cim = Decimal(d["nucleus_im"]) + off * Decimal(repr(math.sin(ang)))
+    return {
+        "center_re": format(cre, "f"),
+        "center_im": format(cim, "f"),
+        "scale": "2" + "0" * k,
+        "width": width,
+        "height": height,
+        "max_iterations": max_iterations,
+        "bailout": bailout,
+        "label": "1e-%d" % k,
+        "period": d["period"],
+    }
+
+
+def c2_views(seed: int = 2, width: int = 1920, height: int = 1080, max_iterations: int = 1_000_000):
+    """The two precision-workload frames (half-widths 1e-300 and 1e-1000)."""
+    return [deep_view(k, seed, width, height, max_iterations) for k in (300, 1000)]
+
+
+if __name__ == "__main__":
+    import sys
+
+    if "--regenerate" in sys.argv:
+        import mbx
+
+        cases = json.load(open(os.path.join(HERE, "..", "tests", "golden", "cases.json")))
+        c = cases["minibrot875"]
+        p, nre, nim, ls = mbx.find_nucleus(c["center_re"], c["center_im"], "1e-600", 100000, 3600)
+        d = nucleus()
+        d.update(nucleus_re=nre, nucleus_im=nim, period=p, size_log10=ls)
+        json.dump(d, open(DATA, "w"), indent=1)
+        print("period", p, "size 1e%.1f" % ls)
