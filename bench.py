@@ -1,0 +1,313 @@
+"""Benchmark: 1080p deep-zoom frames, tuned (mixed-precision) form vs the plain
+FP64 GPU form, at accuracy, with the reference path's CPU restatement timed on
+the host cores beside them.
+
+Workload (one step): the two precision frames — 1920x1080, maxiter 1e6,
+bailout 2^8, half-widths 1e-300 and 1e-1000, centred a seed-drawn 1e-(k+5)
+vector from the Newton-refined period-14164 nucleus (views.c2_views). Inputs are
+synthetic seeded views; the reference publishes no dataset.
+
+  value  : effective pixel-iterations (sum of N, maxiter for interior) per second
+           of the tuned form through the C ABI with device-resident outputs and
+           the per-frame reference orbit/BLA resident (reuse_reference).
+  e2e    : the same metric through the C ABI with host buffers and a fresh
+           reference build (GMP orbit, nucleus search, uploads, D2H) per frame.
+  plain  : the exact FP64 GPU form (reference operation order) on the same frames.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank renders its own replica of the workload (the frames
+are independent; no collective is needed) and rank 0 reports.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mandelbrot-explorer_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "1080p deep-zoom frame ms & Gpixel-iter/s: tuned form vs plain FP64 GPU, at accuracy"
+UNIT = "Gpixel-iter/s"
+FLOPS_PER_STEP = 25  # mp.cpp:2457-2469 + rebase test :2558 (an FMA counts 2)
+FLOPS_PER_BLA = 19   # mp.cpp:2732-2740
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def render(be, mbx, v, mode, device_out=None, reuse=False, width=None, height=None):
+    W = width or v["width"]
+    H = height or v["height"]
+    kw = {}
+    if device_out is not None:
+        kw = dict(iterations=device_out[0], escape_iteration=device_out[1])
+    req = mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], W, H, v["max_iterations"], bailout=v["bailout"], precision_mode=mode, reuse_reference=reuse, **kw)
+    rc = be.compute_status(req)
+    if rc != mbx.OK:
+        raise RuntimeError("render failed (%d): %s" % (rc, be.last_error()))
+    return req, be.last_stats.as_dict()
+
+
+def cpu_reference(views_list, sample_w, sample_h, threads):
+    """The reference path's CPU restatement (oracle port) on a bounded sample:
+    the same views rendered at sample_w x sample_h (same view region, fewer
+    pixels); returns (Gpixel-iter/s, seconds, effective iterations)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    eff = 0
+    t0 = time.perf_counter()
+    for v in views_list:
+        it, _, en, _ = oracle.render(v["center_re"], v["center_im"], v["scale"], sample_w, sample_h, v["max_iterations"], bailout=v["bailout"], threads=threads)
+        eff += int(np.where(en > 0, en, v["max_iterations"]).astype(np.int64).sum())
+    dt = time.perf_counter() - t0
+    return eff / dt / 1e9, dt, eff
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--cpu-sample", default="240x135", help="CPU baseline sample size (same views)")
+    ap.add_argument("--plain-sample", default="480x270", help="plain FP64 GPU sample size (same views); 'full' for 1920x1080")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    import views
+
+    vlist = views.c2_views(width=args.width, height=args.height)
+    sw, sh = (int(x) for x in args.cpu_sample.split("x"))
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        for _ in range(max(1, args.warmup // 3)):
+            cpu_reference(vlist, sw // 2, sh // 2, threads)
+        tot_t, tot_e = 0.0, 0
+        for _ in range(args.steps):
+            v, dt, eff = cpu_reference(vlist, sw, sh, threads)
+            vals.append(v)
+            tot_t += dt
+            tot_e += eff
+        value = tot_e / tot_t / 1e9
+        line = {
+            "impl": "reference",
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": args.gpus,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": tot_t / args.steps * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "C2 deep frames 1e-300 + 1e-1000, sampled at %dx%d of the 1920x1080 view" % (sw, sh), "maxiter": 1000000, "bailout": 256},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": "both C2 views rendered at %dx%d (same view region) per step by the oracle (CPU restatement of the reference path; the reference's AVX2 sources do not build on this Arm host)" % (sw, sh)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import mbx
+
+    be = mbx.create_compute_backend("cuda", local)
+    fp32_peak = be.measure_fma_peak(False)
+    fp64_peak = be.measure_fma_peak(True)
+    W, H = args.width, args.height
+    n = W * H
+    outs = [(torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")) for _ in vlist]
+
+    def step(reuse=True):
+        eff = steps = bla = launches = 0
+        gpu_ms = 0.0
+        per_view = []
+        for v, o in zip(vlist, outs):
+            t = time.perf_counter()
+            _, st = render(be, mbx, v, mbx.PRECISION_MIXED, device_out=o, reuse=reuse)
+            per_view.append((time.perf_counter() - t) * 1e3)
+            eff += st["effective_iterations"]
+            steps += st["steps"]
+            bla += st["bla_applies"]
+            launches += st["kernel_launches"]
+            gpu_ms += st["pass_gpu_ms"]
+        return eff, steps, bla, launches, gpu_ms, per_view
+
+    # warm-up (the first step builds each frame's reference)
+    for _ in range(args.warmup):
+        step(reuse=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tot = [0, 0, 0, 0, 0.0]
+    frame_ms = np.zeros(len(vlist))
+    for _ in range(args.steps):
+        eff, steps, bla, launches, gpu_ms, per_view = step(reuse=True)
+        tot[0] += eff
+        tot[1] += steps
+        tot[2] += bla
+        tot[3] += launches
+        tot[4] += gpu_ms
+        frame_ms += np.array(per_view)
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    ms_per_step = elapsed / args.steps * 1e3
+    value = tot[0] * world / elapsed / 1e9
+
+    # end to end: host buffers, fresh reference per frame, D2H inside
+    e2e_eff, e2e_t, h2d, d2h = 0, 0.0, 0, 0
+    host_frames = []
+    for v in vlist:
+        t = time.perf_counter()
+        req, st = render(be, mbx, v, mbx.PRECISION_MIXED, reuse=False)
+        e2e_t += time.perf_counter() - t
+        e2e_eff += st["effective_iterations"]
+        h2d += st["reference_length"] * 16 * 3 + 64 * 1024  # orbit shadows (+ floatexp shadow) and tables, approx by construction
+        d2h += req.iterations.nbytes + req.escape_iteration.nbytes
+        host_frames.append(req.escape_iteration.copy())
+    e2e_value = e2e_eff / e2e_t / 1e9
+
+    # plain FP64 GPU form on a sample of the same views, and accuracy vs it
+    if args.plain_sample == "full":
+        pw, ph = W, H
+    else:
+        pw, ph = (int(x) for x in args.plain_sample.split("x"))
+    plain_eff, plain_t, agree, total, cls_mis = 0, 0.0, 0, 0, 0
+    plain_frame_ms = []
+    for v in vlist:
+        req_e, st_e = render(be, mbx, v, mbx.PRECISION_EXACT, width=pw, height=ph)
+        req_e2, st_e2 = render(be, mbx, v, mbx.PRECISION_EXACT, width=pw, height=ph, reuse=True)
+        plain_t += st_e2["total_ms"] / 1e3
+        plain_eff += st_e2["effective_iterations"]
+        plain_frame_ms.append(st_e2["total_ms"] * (W * H) / (pw * ph))
+        req_m, _ = render(be, mbx, v, mbx.PRECISION_MIXED, width=pw, height=ph)
+        agree += int(np.sum(req_m.escape_iteration == req_e.escape_iteration))
+        cls_mis += int(np.sum((req_m.escape_iteration < 0) != (req_e.escape_iteration < 0)))
+        total += req_e.escape_iteration.size
+    plain_value = plain_eff / plain_t / 1e9
+
+    # roofline of the dominant kernel (the mixed delta pass), FP32 pipe
+    flops = FLOPS_PER_STEP * tot[1] + FLOPS_PER_BLA * tot[2]
+    achieved = flops / (tot[4] / 1e3) / 1e12 if tot[4] > 0 else 0.0
+
+    cpu = None
+    if rank == 0:
+        sw_, sh_ = sw, sh
+        cpu_v, cpu_dt, cpu_eff = cpu_reference(vlist, sw_, sh_, threads)
+        cpu = {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": "both C2 views at %dx%d (same view region; %.1f s, %.3g pixel-iterations) by the oracle, the CPU restatement of the reference path" % (sw_, sh_, cpu_dt, cpu_eff)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_per_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 (floatexp; f64 decisions)",
+            "data": "synthetic",
+            "config": {
+                "workload": "C2: two 1920x1080 frames (half-width 1e-300 and 1e-1000) at 1e-(k+5) from the period-14164 nucleus, maxiter 1e6, bailout 2^8",
+                "frames_per_step": len(vlist),
+                "resolution": "%dx%d" % (W, H),
+                "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 16.6 MB written per frame; no flush",
+                "frame_ms": {v["label"]: float(ms / args.steps) for v, ms in zip(vlist, frame_ms)},
+            },
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "frame_ms": e2e_t / len(vlist) * 1e3},
+            "plain_fp64": {"value": plain_value, "unit": UNIT, "sample": "%dx%d" % (pw, ph), "frame_ms_scaled_to_1080p": plain_frame_ms},
+            "tuned_vs_plain": value / plain_value if plain_value > 0 else None,
+            "accuracy": {"escape_iteration_identical_vs_exact_fp64": agree / total if total else None, "class_mismatch": cls_mis, "samples": total},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "peak_source": "measured in-run FMA issue rate (mbx_measure_fma_peak); MEASURED_PEAKS.json holds only HBM and bf16", "fp64_peak": fp64_peak},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": tot[3],
+        }
+        print(json.dumps(line))
+    be.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -255,7 +255,7 @@ void Engine::release_device() {
     if (st_) cudaStreamSynchronize(st_);
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
-                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dr2e_.p})
+                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dr2e_.p, (void*)dbla32_.p})
         if (p) cudaFree(p);
     if (dctr_) cudaFree(dctr_);
     if (ev0_) cudaEventDestroy(ev0_);

@@ -191,6 +191,8 @@ class Engine {
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
     DevBuf<int16_t> dr2e_;
+    DevBuf<Bla32> dbla32_;
+    bool mixed_bla32_ = true;
 
     // mixed-pass launch shape (set by the autotuner / defaults)
     int mixed_threads_ = 256;

@@ -30,6 +30,15 @@ struct FE2 {
     FE re, im;
 };
 
+// FP32-floatexp copy of one BLA entry for the mixed-precision pass: A and B as
+// float2 mantissas with one exponent each, radius^2 as mantissa + exponent.
+struct Bla32 {
+    float4 ab; // A.re, A.im (scaled by 2^-ea), B.re, B.im (scaled by 2^-eb)
+    int ea, eb;
+    float r2m; // r2 = r2m * 2^r2e, r2m in [0.5,1); 0 when r2 <= 0
+    int r2e;
+};
+
 // Reference orbit shadows in device memory (mp.h:295-371).
 struct OrbitView {
     const double2* Z;   // Z[k] = (_zfr[k], _zfi[k]); Z[k] is reference value X_{k+1}

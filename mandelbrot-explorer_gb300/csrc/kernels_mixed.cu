@@ -118,6 +118,87 @@ __device__ __forceinline__ void refresh(MixedState& st) {
     st.di = f32e_ratio(st.dci, st.S);
 }
 
+// FP32-floatexp copy of the FP64 BLA table: A and B as float2 mantissas with
+// one exponent each, the radius^2 as float mantissa + exponent. Built once per
+// reference from the FP64 table (k_bla_to_f32).
+__device__ __forceinline__ int dexp_of(double x) { // x = m 2^e, m in [0.5,1)
+    int e;
+    (void)xfrexp(x, &e);
+    return e;
+}
+
+__global__ void k_bla_to_f32(const double* r2, const double4* ab, Bla32* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 c = ab[i];
+    Bla32 b;
+    double amax = fmax(fabs(c.x), fabs(c.y)), bmax = fmax(fabs(c.z), fabs(c.w));
+    b.ea = amax > 0 ? dexp_of(amax) : 0;
+    b.eb = bmax > 0 ? dexp_of(bmax) : 0;
+    b.ab = make_float4((float)xldexp(c.x, -b.ea), (float)xldexp(c.y, -b.ea), (float)xldexp(c.z, -b.eb), (float)xldexp(c.w, -b.eb));
+    double v = r2[i];
+    if (v > 0.0) {
+        int e;
+        double m = xfrexp(v, &e);
+        b.r2m = (float)m;
+        b.r2e = e;
+        if (b.r2m >= 1.0f) { // mantissa rounded up to 1.0
+            b.r2m = 0.5f;
+            b.r2e += 1;
+        }
+    } else {
+        b.r2m = 0.0f;
+        b.r2e = 0;
+    }
+    out[i] = b;
+}
+
+// BLA skip in FP32-floatexp (mp.cpp:2883-2970 semantics; coefficients and
+// radii constructed in FP64). dz = S w, dc = dcm 2^dce (shared exponent).
+__device__ int mixed_bla32(const BlaView& b, const Bla32* t, const float2* orb, bool periodic, int s, F32E& S, float& wr, float& wi, float2 dcm, int dce, float ESC2lo, int mx_ref_it) {
+    int maxp = b.nlev - 1;
+    int startp = (s == 1) ? maxp : __ffs(s - 1) - 1;
+    if (startp > maxp) startp = maxp;
+    if (startp < b.minlevel) return 0;
+    const float wm2 = wr * wr + wi * wi;
+    if (wm2 == 0.0f) return 0;
+    const F32E dz2 = f32e_norm(S.m * S.m * wm2, 2 * S.e);
+    for (int p = startp; p >= b.minlevel; --p) {
+        int i = (s - 1) >> p;
+        if (i >= b.size[p]) continue;
+        const Bla32 e = t[b.off[p] + i];
+        if (e.r2m == 0.0f) continue;
+        if (!(dz2.e < e.r2e || (dz2.e == e.r2e && dz2.m < e.r2m))) continue; // |dz|^2 < r2
+        const int l = 1 << p;
+        const int land = s + l;
+        if (land >= mx_ref_it - 1) continue;
+        // A w 2^(ea + S.e) + B dc 2^(eb + dce)
+        float t1r = e.ab.x * wr - e.ab.y * wi, t1i = e.ab.x * wi + e.ab.y * wr;
+        float t2r = e.ab.z * dcm.x - e.ab.w * dcm.y, t2i = e.ab.z * dcm.y + e.ab.w * dcm.x;
+        const int E1 = e.ea + S.e, E2 = e.eb + dce;
+        const int E = max(E1, E2);
+        const float vr = ldexpf_ftz(t1r, E1 - E) + ldexpf_ftz(t2r, E2 - E);
+        const float vi = ldexpf_ftz(t1i, E1 - E) + ldexpf_ftz(t2i, E2 - E);
+        const float v2 = vr * vr + vi * vi;
+        // Never skip past an escape: z = X_land + dz' (conservative FP32 test).
+        const float2 zl = orb[land];
+        const float zr = zl.x + ldexpf_ftz(vr, E), zi = zl.y + ldexpf_ftz(vi, E);
+        if (zr * zr + zi * zi > ESC2lo) return 0;
+        if (v2 == 0.0f) {
+            if (!periodic) return 0;
+            S = F32E{0.5f, 1};
+            wr = wi = 0.0f;
+        } else {
+            const float vm = sqrtf(v2), inv = 1.0f / vm;
+            S = f32e_norm(vm, E);
+            wr = vr * inv;
+            wi = vi * inv;
+        }
+        return l;
+    }
+    return 0;
+}
+
 // BLA skip (mp.cpp:2883-2970 semantics): levels screened on integer exponents
 // of |dz|^2 against the precomputed exponents of r2; decided and applied in FP64.
 __device__ int mixed_bla(const BlaView& b, const int16_t* r2e, const double2* Z, bool periodic, int s, MixedState& st, FE dcr, FE dci, double ESC2, int mx_ref_it) {
@@ -195,7 +276,7 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
     return done != 0;
 }
 
-__global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e) {
+__global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e, const Bla32* bla32) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ unsigned long long mbar;
     __shared__ int stage_ok;
@@ -244,6 +325,9 @@ __global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p
         MixedState st;
         st.dcr = f32e_from_fe(dcr);
         st.dci = f32e_from_fe(dci);
+        int dce = max(st.dcr.m != 0.0f ? st.dcr.e : -2147483000, st.dci.m != 0.0f ? st.dci.e : -2147483000);
+        if (dce < -2000000000) dce = 0;
+        const float2 dcm = make_float2(ldexpf_ftz(st.dcr.m, st.dcr.e - dce), ldexpf_ftz(st.dci.m, st.dci.e - dce));
         {
             FE S0 = fe_sqrt(fe_add(fe_mul(dcr, dcr), fe_mul(dci, dci)));
             if (S0.m == 0.0) {
@@ -267,13 +351,36 @@ __global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p
         int outcome = 0, nesc = -1;
         double zrad_d = 0.0;
         int tick = 0;
+        // Exact state repetition (the reference's int_rep, mp.cpp:3362-3383):
+        // the state (reference index, S, w) determines the future, so its exact
+        // recurrence proves a cycle. With a periodic reference the index is
+        // taken modulo the period (the mixed form's extension).
+        float swr = 3e38f, swi = 3e38f;
+        F32E sS = F32E{2.0f, 0};
+        int sidx = -2, save_iter2 = 1, twin2 = 1;
         while (iter < g.mxit) {
             if (((++tick) & 8191) == 0 && mcancelled(f)) {
                 outcome = 4;
                 break;
             }
+            if (p.use_interior) {
+                const int idxs = per ? rm : m;
+                if (idxs == sidx && st.wr == swr && st.wi == swi && st.S.m == sS.m && st.S.e == sS.e) {
+                    outcome = 2;
+                    break;
+                }
+                if (iter - save_iter2 >= twin2) {
+                    swr = st.wr;
+                    swi = st.wi;
+                    sS = st.S;
+                    sidx = idxs;
+                    save_iter2 = iter;
+                    twin2 += twin2;
+                }
+            }
             if (f.bla.use && m >= 2 && ((rm - 1) & blamask) == 0) {
-                int skip = mixed_bla(f.bla, r2e, Zd, per > 0, rm, st, dcr, dci, g.ESC2, per ? per : reflen);
+                int skip = bla32 ? mixed_bla32(f.bla, bla32, orb, per > 0, rm, st.S, st.wr, st.wi, dcm, dce, ESC2lo, per ? per : reflen)
+                                 : mixed_bla(f.bla, r2e, Zd, per > 0, rm, st, dcr, dci, g.ESC2, per ? per : reflen);
                 if (skip > 0) {
                     ++n_bla;
                     n_skip += skip;
@@ -526,6 +633,9 @@ int Engine::prepare_mixed() {
         if (!ensure(dr2e_, (size_t)n)) return MBX_E_NOMEM;
         k_bla_exponents<<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dr2e_.p, n);
         ++stats_.kernel_launches;
+        if (!ensure(dbla32_, (size_t)n)) return MBX_E_NOMEM;
+        k_bla_to_f32<<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbla32_.p, n);
+        ++stats_.kernel_launches;
     }
     return cuda_ok("mixed preparation");
 }
@@ -556,7 +666,7 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
     }
     DeviceFrame g = f;
     if (!(bla_.use && dr2e_.p)) g.bla.use = 0;
-    k_mixed_pass<<<blocks, threads, smem, st_>>>(g, p, dr2e_.p);
+    k_mixed_pass<<<blocks, threads, smem, st_>>>(g, p, dr2e_.p, mixed_bla32_ ? dbla32_.p : nullptr);
     return cudaGetLastError();
 }
 

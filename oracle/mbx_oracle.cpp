@@ -374,6 +374,9 @@ class Engine {
         for (int i = 0; i < 2; ++i) { mpf_set_prec(zre[i], p); mpf_set_prec(zim[i], p); }
     }
     void compute(mpf_srcptr cre, mpf_srcptr cim, mpf_srcptr scale, int mxit, int cm, int full_h, int row_base);
+    // Brute-force arbitrary-precision value of listed samples on the frame
+    // grid (ComputeDirect semantics, mp.cpp:959-990, at `wp` bits).
+    void truth(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int full_h, int row_base, int mxit, int cm, const int* keys, int n, int wp, float* out, int* nout);
 
     long long stat_steps = 0, stat_bla = 0, stat_skipped = 0, stat_passes = 0, stat_refs = 0, stat_gmp = 0;
     int method = 0;
@@ -2022,6 +2025,58 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
     }
 }
 
+void Engine::truth(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int full_h, int row_base, int mxit, int cm, const int* keys, int n, int wp, float* out, int* nout) {
+    // Same grid as compute() (mp.cpp:1403-1424).
+    int rows = (full_h > 0) ? full_h : H;
+    mpf_t dw, dh;
+    mpf_init_set_ui(dw, 2);
+    mpf_div(dw, dw, scale);
+    mpf_init_set(dh, dw);
+    mpf_div_ui(dh, dh, W);
+    mpf_mul_ui(dh, dh, rows);
+    mpf_sub(c0_re, c_re, dw);
+    mpf_sub(c0_im, c_im, dh);
+    mpf_div_ui(dx, dw, W - 1);
+    mpf_mul_ui(dx, dx, 2);
+    mpf_div_ui(dy, dh, rows - 1);
+    mpf_mul_ui(dy, dy, 2);
+    if (row_base > 0) {
+        mpf_t off;
+        mpf_init(off);
+        mpf_mul_ui(off, dy, row_base);
+        mpf_add(c0_im, c0_im, off);
+        mpf_clear(off);
+    }
+    mpf_clear(dw);
+    mpf_clear(dh);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < n; ++q) {
+        mpf_t cre, cim, off, soff;
+        mpf_init2(cre, wp); mpf_init2(cim, wp); mpf_init2(off, wp); mpf_init2(soff, wp);
+        const int* a = keys + 4 * q;
+        mpf_set(cre, c0_re);
+        mpf_set(cim, c0_im);
+        mpf_mul_ui(off, dx, a[1]);
+        mpf_add(cre, cre, off);
+        mpf_mul_ui(off, dx, std::abs(a[3]));
+        mpf_set(soff, off);
+        if (a[3] < 0) mpf_neg(soff, soff);
+        mpf_div_ui(soff, soff, SUB);
+        mpf_add(cre, cre, soff);
+        mpf_mul_ui(off, dy, a[0]);
+        mpf_add(cim, cim, off);
+        mpf_mul_ui(off, dy, std::abs(a[2]));
+        mpf_set(soff, off);
+        if (a[2] < 0) mpf_neg(soff, soff);
+        mpf_div_ui(soff, soff, SUB);
+        mpf_add(cim, cim, soff);
+        int nn = -1;
+        out[q] = accuratePoint(cre, cim, mxit, cm, &nn);
+        if (nout) nout[q] = nn;
+        mpf_clears(cre, cim, off, soff, (mpf_ptr)0);
+    }
+}
+
 // mp.cpp:1388-2028 (Mandelbrot mode).
 void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxit, int cm, int full_h, int row_base) {
     mpf_set(scale_, scale);
@@ -2229,6 +2284,32 @@ int mbx_oracle_render(const char* cx, const char* cy, const char* scale_digits, 
             stats[6] = e.method;
             stats[7] = 0;
         }
+    }
+    mpf_clear(mcx);
+    mpf_clear(mcy);
+    mpf_clear(msc);
+    return 0;
+}
+
+// Arbitrary-precision ground truth for listed samples (keys: n x {row, col,
+// subrow, subcol}) of a frame, iterated at work_bits of precision with the
+// reference's per-pixel GMP iteration (accuratePointCompute, mp.cpp:719-894).
+int mbx_oracle_truth(const char* cx, const char* cy, const char* scale_digits, int prec_bits, int work_bits, int W, int H, int mxit, int sub, int cmethod, double bailout, int full_h, int row_base, int threads, const int* keys, int n, float* out, int32_t* nout) {
+    if (W < 2 || H < 1 || mxit < 1 || sub < 1 || !keys || !out) return -1;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    mpf_set_default_prec((mp_bitcnt_t)prec_bits);
+    mpf_t mcx, mcy, msc;
+    mpf_init_set_str(mcx, cx, 10);
+    mpf_init_set_str(mcy, cy, 10);
+    mpf_init_set_str(msc, scale_digits, 10);
+    Opts o;
+    std::vector<float> dummy(1);
+    {
+        Engine e(W, H, mxit, sub, dummy.data(), nullptr, nullptr, bailout, o);
+        e.setPrecision(prec_bits);
+        e.truth(mcx, mcy, msc, full_h, row_base, mxit, cmethod, keys, n, work_bits > 0 ? work_bits : prec_bits, out, nout);
     }
     mpf_clear(mcx);
     mpf_clear(mcy);

@@ -24,6 +24,8 @@ def load():
         lib = ctypes.CDLL(path)
         lib.mbx_oracle_render.restype = ctypes.c_int
         lib.mbx_oracle_render.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 6 + [ctypes.c_double] + [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4
+        lib.mbx_oracle_truth.restype = ctypes.c_int
+        lib.mbx_oracle_truth.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 7 + [ctypes.c_double] + [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         _lib = lib
     return _lib
 
@@ -47,3 +49,18 @@ def render(center_re, center_im, scale, width, height, max_iterations, sub=1, co
         raise ValueError("oracle rejected the request (%d)" % rc)
     keys = ("steps", "bla_applies", "bla_skipped", "passes", "references", "gmp_pixels", "method")
     return it, nr, en, dict(zip(keys, (int(x) for x in st)))
+
+
+def truth(center_re, center_im, scale, width, height, max_iterations, keys, sub=1, coloring_method=0, bailout=1e8, full_height=0, row_base=0, threads=0, precision_bits=0, work_bits=0):
+    """Arbitrary-precision brute-force value and escape iteration of the listed
+    samples (keys: (n, 4) int array of row, col, subrow, subcol)."""
+    lib = load()
+    keys = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1, 4))
+    n = keys.shape[0]
+    out = np.empty(n, np.float32)
+    nout = np.empty(n, np.int32)
+    prec = precision_bits or precision_for_scale(scale)
+    rc = lib.mbx_oracle_truth(center_re.encode(), center_im.encode(), scale.encode(), prec, work_bits or prec, width, height, max_iterations, sub, coloring_method, float(bailout), full_height, row_base, threads, keys.ctypes.data, n, out.ctypes.data, nout.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle truth rejected the request")
+    return out, nout
