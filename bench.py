@@ -125,7 +125,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--cpu-sample", default="240x135", help="CPU baseline sample size (same views)")
+    ap.add_argument("--cpu-sample", default="1920x1080", help="cpu_baseline sample size (same views); one render of each")
+    ap.add_argument("--ref-sample", default="960x540", help="--impl reference per-step sample size (same views)")
     ap.add_argument("--plain-sample", default="480x270", help="plain FP64 GPU sample size (same views); 'full' for 1920x1080")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -138,6 +139,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        sw, sh = (int(x) for x in args.ref_sample.split("x"))
         vals = []
         for _ in range(max(1, args.warmup // 3)):
             cpu_reference(vlist, sw // 2, sh // 2, threads)
@@ -181,6 +183,8 @@ def main():
     be = mbx.create_compute_backend("cuda", local)
     fp32_peak = be.measure_fma_peak(False)
     fp64_peak = be.measure_fma_peak(True)
+    # one context per frame: each keeps its own resident reference orbit / BLA table
+    ctxs = [mbx.create_compute_backend("cuda", local) for _ in vlist]
     W, H = args.width, args.height
     n = W * H
     outs = [(torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")) for _ in vlist]
@@ -189,9 +193,9 @@ def main():
         eff = steps = bla = launches = 0
         gpu_ms = 0.0
         per_view = []
-        for v, o in zip(vlist, outs):
+        for v, o, cx in zip(vlist, outs, ctxs):
             t = time.perf_counter()
-            _, st = render(be, mbx, v, mbx.PRECISION_MIXED, device_out=o, reuse=reuse)
+            _, st = render(cx, mbx, v, mbx.PRECISION_MIXED, device_out=o, reuse=reuse)
             per_view.append((time.perf_counter() - t) * 1e3)
             eff += st["effective_iterations"]
             steps += st["steps"]
@@ -304,6 +308,8 @@ def main():
             "gpu_launches": tot[3],
         }
         print(json.dumps(line))
+    for cx in ctxs:
+        cx.close()
     be.close()
     if world > 1:
         dist.destroy_process_group()

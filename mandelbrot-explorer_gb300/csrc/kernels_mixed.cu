@@ -172,8 +172,9 @@ __device__ int mixed_bla32(const BlaView& b, const Bla32* t, const float2* orb, 
         const int l = 1 << p;
         const int land = s + l;
         if (land >= mx_ref_it - 1) continue;
-        // A w 2^(ea + S.e) + B dc 2^(eb + dce)
-        float t1r = e.ab.x * wr - e.ab.y * wi, t1i = e.ab.x * wi + e.ab.y * wr;
+        // A dz + B dc = A (S.m w) 2^(ea + S.e) + B dcm 2^(eb + dce)
+        const float swr = S.m * wr, swi = S.m * wi;
+        float t1r = e.ab.x * swr - e.ab.y * swi, t1i = e.ab.x * swi + e.ab.y * swr;
         float t2r = e.ab.z * dcm.x - e.ab.w * dcm.y, t2i = e.ab.z * dcm.y + e.ab.w * dcm.x;
         const int E1 = e.ea + S.e, E2 = e.eb + dce;
         const int E = max(E1, E2);
