@@ -277,10 +277,297 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
     return done != 0;
 }
 
-__global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e, const Bla32* bla32) {
+// Per-lane state of the mixed pass.
+struct Lane {
+    int i, oidx;         // pass entry, output index
+    double dpx, dpy;     // sample offset from the reference in pixels (for rare exact steps)
+    F32E S;              // delta scale
+    float wr, wi, s, dr, di;
+    float2 dcm;          // dc mantissas with shared exponent dce
+    int dce;
+    int m, iter, rm;
+    float2 Xc;           // X_m
+    // interior detection
+    float zsr_f, zsi_f, conf_D2, swr, swi;
+    double zsr, zsi, conf_zr, conf_zi;
+    F32E sS;
+    int save_iter, period_win, conf_P, conf_next, conf_count, conf_giveup, sidx, save_iter2, twin2;
+};
+
+__device__ __forceinline__ void lane_refresh(Lane& L) {
+    L.s = f32e_to_float(L.S);
+    const float inv = __fdividef(1.0f, L.S.m);
+    L.dr = ldexpf_ftz(L.dcm.x * inv, L.dce - L.S.e);
+    L.di = ldexpf_ftz(L.dcm.y * inv, L.dce - L.S.e);
+}
+
+// dz = S w with S <- |v| 2^e and w <- v / |v| for an FP32 vector v scaled by 2^e.
+__device__ __forceinline__ void lane_set_delta(Lane& L, float vr, float vi, int e) {
+    const float v2 = vr * vr + vi * vi;
+    if (v2 == 0.0f) {
+        L.S = F32E{0.5f, 1};
+        L.wr = L.wi = 0.0f;
+        return;
+    }
+    const float vm = sqrtf(v2), inv = 1.0f / vm;
+    L.S = f32e_norm(vm, e);
+    L.wr = vr * inv;
+    L.wi = vi * inv;
+}
+
+__device__ __forceinline__ FE lane_dc_re(const MixedParams& p, const Lane& L) { return fe_mul_d(p.dxfe, L.dpx); }
+__device__ __forceinline__ FE lane_dc_im(const MixedParams& p, const Lane& L) { return fe_mul_d(p.dyfe, L.dpy); }
+
+__device__ void lane_setup(Lane& L, int i, const DeviceFrame& f, const MixedParams& p, const F32E dxf, const F32E dyf, const float2* orb) {
+    const FrameGeom& g = p.g;
+    int arr[4];
+    if (f.px.keys) {
+        key_unpack(f.px.keys[i], arr);
+    } else {
+        int cols = (f.px.grid_w + f.px.grid_step - 1) / f.px.grid_step;
+        int q = i;
+        if (f.px.skip_i >= 0) {
+            int sq = (f.px.skip_i / f.px.grid_step) * cols + f.px.skip_j / f.px.grid_step;
+            if (q >= sq) ++q;
+        }
+        arr[0] = (q / cols) * f.px.grid_step;
+        arr[1] = (q % cols) * f.px.grid_step;
+        arr[2] = arr[3] = 0;
+    }
+    L.i = i;
+    L.oidx = (arr[0] * g.sub + g.sub / 2 + arr[2]) * g.W * g.sub + (arr[1] * g.sub + g.sub / 2 + arr[3]);
+    L.dpx = arr[1] + (double)arr[3] / g.sub - p.ref_x;
+    L.dpy = arr[0] + (double)arr[2] / g.sub - p.ref_y;
+    // dc in FP32 floatexp with one shared exponent.
+    const F32E cr = f32e_mulf(dxf, (float)L.dpx), ci = f32e_mulf(dyf, (float)L.dpy);
+    int e = (cr.m != 0.0f) ? cr.e : ((ci.m != 0.0f) ? ci.e : 0);
+    if (cr.m != 0.0f && ci.m != 0.0f) e = max(cr.e, ci.e);
+    L.dce = e;
+    L.dcm = make_float2(ldexpf_ftz(cr.m, cr.e - e), ldexpf_ftz(ci.m, ci.e - e));
+    lane_set_delta(L, L.dcm.x, L.dcm.y, e);
+    lane_refresh(L);
+    L.m = 1;
+    L.iter = 1;
+    L.rm = 0;
+    L.Xc = orb[0];
+    L.zsr = L.zsi = 1e30;
+    L.zsr_f = L.zsi_f = 1e30f;
+    L.conf_zr = L.conf_zi = 0.0;
+    L.conf_D2 = 0.0f;
+    L.save_iter = 1;
+    L.period_win = 1;
+    L.conf_P = L.conf_next = L.conf_count = L.conf_giveup = 0;
+    L.swr = L.swi = 3e38f;
+    L.sS = F32E{2.0f, 0};
+    L.sidx = -2;
+    L.save_iter2 = 1;
+    L.twin2 = 1;
+}
+
+// z = X_m + S w in FP64 (rare decisions).
+__device__ __forceinline__ void lane_z_double(const Lane& L, const double2* Zd, double& zr, double& zi) {
+    const double2 Xd = L.m ? Zd[L.rm] : make_double2(0.0, 0.0);
+    const double sd = xldexp((double)L.S.m, L.S.e);
+    zr = Xd.x + sd * (double)L.wr;
+    zi = Xd.y + sd * (double)L.wi;
+}
+
+// Advance one lane by up to `budget` iterations. Returns 0 running, 1 escaped,
+// 2 interior, 4 cancelled; nesc / zrad_out are set on escape.
+__device__ int lane_run(Lane& L, int budget, const DeviceFrame& f, const MixedParams& p, const Bla32* bla32, const float2* orb, int reflen, float ESC2f, int blamask, float& zrad_out, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip, unsigned long long& n_rebase) {
+    const FrameGeom& g = p.g;
+    const int per = p.per;
+    const double2* Zd = f.orbit.Z;
+    const FE2* Zfe = f.orbit.Zfe;
+    const float ESC2hi = ESC2f * 1.000002f, ESC2lo = ESC2f * 0.999998f;
+    for (int b = 0; b < budget; ++b) {
+        if (L.iter >= g.mxit) return 2;
+        if (p.use_interior) {
+            const int idxs = per ? L.rm : L.m;
+            if (idxs == L.sidx && L.wr == L.swr && L.wi == L.swi && L.S.m == L.sS.m && L.S.e == L.sS.e) return 2;
+            if (L.iter - L.save_iter2 >= L.twin2) {
+                L.swr = L.wr;
+                L.swi = L.wi;
+                L.sS = L.S;
+                L.sidx = idxs;
+                L.save_iter2 = L.iter;
+                L.twin2 += L.twin2;
+            }
+        }
+        if (bla32 && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
+            const int skip = mixed_bla32(f.bla, bla32, orb, per > 0, L.rm, L.S, L.wr, L.wi, L.dcm, L.dce, ESC2lo, per ? per : reflen);
+            if (skip > 0) {
+                ++n_bla;
+                n_skip += skip;
+                L.m += skip;
+                L.iter += skip;
+                L.rm += skip;
+                if (per && L.rm >= per) L.rm -= per;
+                lane_refresh(L);
+                L.Xc = orb[L.rm];
+                L.zsr = L.zsi = 1e30;
+                L.zsr_f = L.zsi_f = 1e30f;
+                L.save_iter = L.iter;
+                L.period_win = 1;
+                L.conf_P = 0;
+                L.conf_giveup = 0;
+                continue;
+            }
+        }
+        ++n_steps;
+        // w' = (2 X_m + s w) w + d
+        const bool tiny = L.m != 0 && fabsf(L.Xc.x) < 1e-30f && fabsf(L.Xc.y) < 1e-30f && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0);
+        if (!tiny) {
+            const float fR = 2.0f * L.Xc.x + L.s * L.wr;
+            const float fI = 2.0f * L.Xc.y + L.s * L.wi;
+            const float nwr = fR * L.wr - fI * L.wi + L.dr;
+            const float nwi = fR * L.wi + fI * L.wr + L.di;
+            L.wr = nwr;
+            L.wi = nwi;
+        } else {
+            double wr = L.wr, wi = L.wi;
+            FE S = fe_from_f32e(L.S);
+            exact_step(Zfe[L.rm].re, Zfe[L.rm].im, lane_dc_re(p, L), lane_dc_im(p, L), S, wr, wi);
+            const double mg = sqrt(wr * wr + wi * wi);
+            L.S = f32e_from_fe(S);
+            L.wr = (float)wr;
+            L.wi = (float)wi;
+            (void)mg;
+            lane_refresh(L);
+        }
+        ++L.m;
+        ++L.iter;
+        ++L.rm;
+        if (per && L.rm == per) L.rm = 0;
+        L.Xc = orb[L.rm];
+        const float zr = L.Xc.x + L.s * L.wr, zi = L.Xc.y + L.s * L.wi;
+        const float zrad = zr * zr + zi * zi;
+        if (zrad > ESC2lo) {
+            if (zrad > ESC2hi) {
+                zrad_out = zrad;
+                return 1;
+            }
+            double zdr, zdi;
+            lane_z_double(L, Zd, zdr, zdi);
+            const double zr2 = zdr * zdr + zdi * zdi;
+            if (zr2 > g.ESC2) {
+                zrad_out = (float)zr2;
+                return 1;
+            }
+        }
+        if (p.use_interior) {
+            if (L.conf_P > 0) {
+                L.conf_D2 *= 4.0f * zrad;
+                if (L.conf_D2 > 1e18f) L.conf_D2 = 1e18f;
+                if (L.iter >= L.conf_next) {
+                    double zdr, zdi;
+                    lane_z_double(L, Zd, zdr, zdi);
+                    const double qr = zdr - L.conf_zr, qi = zdi - L.conf_zi;
+                    if (qr * qr + qi * qi < p.interior_eps2 * (zdr * zdr + zdi * zdi) && L.conf_D2 < 1.0f) {
+                        if (++L.conf_count >= p.interior_confirm) return 2;
+                        L.conf_zr = zdr;
+                        L.conf_zi = zdi;
+                        L.conf_D2 = 1.0f;
+                        L.conf_next = L.iter + L.conf_P;
+                    } else {
+                        L.conf_P = 0;
+                        ++L.conf_giveup;
+                    }
+                }
+            } else if ((L.iter & 15) == 0 && L.conf_giveup < 3) {
+                const float qr = zr - L.zsr_f, qi = zi - L.zsi_f;
+                const bool maybe = qr * qr + qi * qi < 1e-11f * zrad;
+                const bool save = L.iter - L.save_iter >= L.period_win;
+                if (maybe || save) {
+                    double zdr, zdi;
+                    lane_z_double(L, Zd, zdr, zdi);
+                    if (maybe) {
+                        const double dqr = zdr - L.zsr, dqi = zdi - L.zsi;
+                        if (dqr * dqr + dqi * dqi < p.interior_eps2 * (zdr * zdr + zdi * zdi)) {
+                            L.conf_P = max(L.iter - L.save_iter, 1);
+                            L.conf_zr = zdr;
+                            L.conf_zi = zdi;
+                            L.conf_D2 = 1.0f;
+                            L.conf_next = L.iter + L.conf_P;
+                            L.conf_count = 0;
+                        }
+                    }
+                    if (save) {
+                        L.zsr = zdr;
+                        L.zsi = zdi;
+                        L.zsr_f = zr;
+                        L.zsi_f = zi;
+                        L.save_iter = L.iter;
+                        L.period_win += L.period_win;
+                    }
+                }
+            }
+        }
+        // keep |w| ~ 1
+        const float wm2 = L.wr * L.wr + L.wi * L.wi;
+        if (wm2 > 1e16f || (wm2 < 1e-16f && wm2 > 0.0f)) {
+            const float wmag = sqrtf(wm2), inv = 1.0f / wmag;
+            L.S = f32e_mulf(L.S, wmag);
+            L.wr *= inv;
+            L.wi *= inv;
+            lane_refresh(L);
+        }
+        // Rebase (mp.cpp:3584-3615): |z|^2 < |dz|^2 decided on FP32 floatexp
+        // with a 1e-4 margin; FP64 floatexp inside the margin, for strong
+        // cancellation in X + dz, and at the end of the reference.
+        const float w2 = L.wr * L.wr + L.wi * L.wi;
+        const F32E dz2 = f32e_norm(L.S.m * L.S.m * w2, 2 * L.S.e);
+        int decide = 0; // 0 none, 1 rebase in FP32, 2 FP64 test
+        if (!per && L.m >= reflen) decide = 2;
+        else if (dz2.m != 0.0f) {
+            if (zrad == 0.0f) decide = 2;
+            else {
+                const F32E z2 = f32e_norm(zrad, 0);
+                const float q = ldexpf_ftz(__fdividef(z2.m, dz2.m), max(-120, min(120, z2.e - dz2.e)));
+                if (q < 0.9999f) decide = (zrad > 1e-6f * (L.Xc.x * L.Xc.x + L.Xc.y * L.Xc.y) && L.s != 0.0f) ? 1 : 2;
+                else if (q < 1.0001f) decide = 2;
+            }
+        }
+        if (decide == 1) {
+            lane_set_delta(L, zr, zi, 0);
+            lane_refresh(L);
+            L.m = 0;
+            L.rm = -1;
+            L.Xc = make_float2(0.0f, 0.0f);
+            ++n_rebase;
+        } else if (decide == 2) {
+            const FE S = fe_from_f32e(L.S);
+            FE Xmr = L.m ? Zfe[L.rm].re : fe_make(0.0, 0);
+            FE Xmi = L.m ? Zfe[L.rm].im : fe_make(0.0, 0);
+            FE Swr = fe_mul_d(S, (double)L.wr), Swi = fe_mul_d(S, (double)L.wi);
+            FE zrfe = fe_add(Xmr, Swr), zife = fe_add(Xmi, Swi);
+            FE zradfe = fe_add(fe_mul(zrfe, zrfe), fe_mul(zife, zife));
+            FE dzfe = fe_add(fe_mul(Swr, Swr), fe_mul(Swi, Swi));
+            if ((!per && L.m >= reflen) || fe_abs_less(zradfe, dzfe)) {
+                FE Snew = fe_sqrt(zradfe);
+                if (Snew.m == 0.0) {
+                    L.wr = L.wi = 0.0f;
+                } else {
+                    L.S = f32e_from_fe(Snew);
+                    L.wr = (float)fe_to_double(fe_div(zrfe, Snew));
+                    L.wi = (float)fe_to_double(fe_div(zife, Snew));
+                    lane_refresh(L);
+                }
+                L.m = 0;
+                L.rm = -1;
+                L.Xc = make_float2(0.0f, 0.0f);
+                ++n_rebase;
+            }
+        }
+    }
+    return 0;
+}
+
+__global__ void __launch_bounds__(256, 2) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e, const Bla32* bla32) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ unsigned long long mbar;
     __shared__ int stage_ok;
+    (void)r2e;
     const FrameGeom& g = p.g;
     const float2* orb = p.Zf;
     if (p.orbit_in_smem) {
@@ -288,260 +575,67 @@ __global__ void __launch_bounds__(256) k_mixed_pass(DeviceFrame f, MixedParams p
         bool ok = stage_orbit(so, p.Zf, p.smem_entries, &mbar);
         if (threadIdx.x == 0) stage_ok = ok ? 1 : 0;
         __syncthreads();
-        if (stage_ok) orb = so;
-        else if (threadIdx.x == 0) atomicAdd(&f.ctr->rescales, 1ull); // staging timed out: global reads
-        if (!stage_ok) return; // an in-flight copy must not land in a reused CTA slot; leave the work to other blocks
+        if (!stage_ok) {
+            if (threadIdx.x == 0) atomicAdd(&f.ctr->rescales, 1ull); // staging timed out: this block leaves its share to the others
+            return;
+        }
+        orb = so;
     }
-    const double2* Zd = f.orbit.Z;
-    const FE2* Zfe = f.orbit.Zfe;
     const int reflen = p.mx_ref_it + 1;
-    const int per = p.per;
     const float ESC2f = (float)g.ESC2;
-    const float ESC2lo = ESC2f * 0.99999f;
     const int blamask = (1 << f.bla.minlevel) - 1;
+    const Bla32* bt = f.bla.use ? bla32 : nullptr;
+    const F32E dxf = f32e_from_fe(p.dxfe), dyf = f32e_from_fe(p.dyfe);
+    const unsigned lane_id = threadIdx.x & 31;
     unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0;
     unsigned int n_int = 0;
+    Lane L;
+    bool live = false, exhausted = false, stop = false;
+    unsigned rounds = 0;
     for (;;) {
-        if (mcancelled(f)) break;
-        int i = (int)atomicAdd(&f.ctr->next, 1u);
-        if (i >= f.px.n) break;
-        int arr[4];
-        if (f.px.keys) {
-            key_unpack(f.px.keys[i], arr);
-        } else {
-            int cols = (f.px.grid_w + f.px.grid_step - 1) / f.px.grid_step;
-            int q = i;
-            if (f.px.skip_i >= 0) {
-                int sq = (f.px.skip_i / f.px.grid_step) * cols + f.px.skip_j / f.px.grid_step;
-                if (q >= sq) ++q;
-            }
-            arr[0] = (q / cols) * f.px.grid_step;
-            arr[1] = (q % cols) * f.px.grid_step;
-            arr[2] = arr[3] = 0;
-        }
-        const double px = arr[1] + (double)arr[3] / g.sub;
-        const double py = arr[0] + (double)arr[2] / g.sub;
-        const FE dcr = fe_mul_d(p.dxfe, px - p.ref_x);
-        const FE dci = fe_mul_d(p.dyfe, py - p.ref_y);
-        MixedState st;
-        st.dcr = f32e_from_fe(dcr);
-        st.dci = f32e_from_fe(dci);
-        int dce = max(st.dcr.m != 0.0f ? st.dcr.e : -2147483000, st.dci.m != 0.0f ? st.dci.e : -2147483000);
-        if (dce < -2000000000) dce = 0;
-        const float2 dcm = make_float2(ldexpf_ftz(st.dcr.m, st.dcr.e - dce), ldexpf_ftz(st.dci.m, st.dci.e - dce));
-        {
-            FE S0 = fe_sqrt(fe_add(fe_mul(dcr, dcr), fe_mul(dci, dci)));
-            if (S0.m == 0.0) {
-                st.S = F32E{0.5f, 1};
-                st.wr = st.wi = 0.0f;
-            } else {
-                st.S = f32e_from_fe(S0);
-                st.wr = (float)fe_to_double(fe_div(dcr, S0));
-                st.wi = (float)fe_to_double(fe_div(dci, S0));
-            }
-        }
-        refresh(st);
-        int m = 1, iter = 1, rm = 0;
-        float2 Xc = make_float2(0.0f, 0.0f); // X_m (X_0 = 0)
-        Xc = orb[0];                          // m = 1 -> stored index 0
-        // Brent interior detector (mp.cpp:3533-3568), FP32 screen + FP64 confirm.
-        double zsr = 1e30, zsi = 1e30, conf_zr = 0, conf_zi = 0;
-        float zsr_f = 1e30f, zsi_f = 1e30f;
-        float conf_D2 = 0.0f;
-        int save_iter = 1, period_win = 1, conf_P = 0, conf_next = 0, conf_count = 0, conf_giveup = 0;
-        int outcome = 0, nesc = -1;
-        double zrad_d = 0.0;
-        int tick = 0;
-        // Exact state repetition (the reference's int_rep, mp.cpp:3362-3383):
-        // the state (reference index, S, w) determines the future, so its exact
-        // recurrence proves a cycle. With a periodic reference the index is
-        // taken modulo the period (the mixed form's extension).
-        float swr = 3e38f, swi = 3e38f;
-        F32E sS = F32E{2.0f, 0};
-        int sidx = -2, save_iter2 = 1, twin2 = 1;
-        while (iter < g.mxit) {
-            if (((++tick) & 8191) == 0 && mcancelled(f)) {
-                outcome = 4;
-                break;
-            }
-            if (p.use_interior) {
-                const int idxs = per ? rm : m;
-                if (idxs == sidx && st.wr == swr && st.wi == swi && st.S.m == sS.m && st.S.e == sS.e) {
-                    outcome = 2;
-                    break;
-                }
-                if (iter - save_iter2 >= twin2) {
-                    swr = st.wr;
-                    swi = st.wi;
-                    sS = st.S;
-                    sidx = idxs;
-                    save_iter2 = iter;
-                    twin2 += twin2;
-                }
-            }
-            if (f.bla.use && m >= 2 && ((rm - 1) & blamask) == 0) {
-                int skip = bla32 ? mixed_bla32(f.bla, bla32, orb, per > 0, rm, st.S, st.wr, st.wi, dcm, dce, ESC2lo, per ? per : reflen)
-                                 : mixed_bla(f.bla, r2e, Zd, per > 0, rm, st, dcr, dci, g.ESC2, per ? per : reflen);
-                if (skip > 0) {
-                    ++n_bla;
-                    n_skip += skip;
-                    m += skip;
-                    iter += skip;
-                    rm += skip;
-                    if (per && rm >= per) rm -= per;
-                    refresh(st);
-                    Xc = orb[rm];
-                    zsr = zsi = 1e30;
-                    zsr_f = zsi_f = 1e30f;
-                    save_iter = iter;
-                    period_win = 1;
-                    conf_P = 0;
-                    conf_giveup = 0;
-                    continue;
-                }
-            }
-            ++n_steps;
-            // w' = (2 X_m + s w) w + d   (X_0 = 0 after a rebase)
-            const bool tiny = m != 0 && fabsf(Xc.x) < 1e-30f && fabsf(Xc.y) < 1e-30f && (Zfe[rm].re.m != 0.0 || Zfe[rm].im.m != 0.0);
-            if (!tiny) {
-                const float fR = 2.0f * Xc.x + st.s * st.wr;
-                const float fI = 2.0f * Xc.y + st.s * st.wi;
-                const float nwr = fR * st.wr - fI * st.wi + st.dr;
-                const float nwi = fR * st.wi + fI * st.wr + st.di;
-                st.wr = nwr;
-                st.wi = nwi;
-            } else {
-                double wr = st.wr, wi = st.wi;
-                FE S = fe_from_f32e(st.S);
-                exact_step(Zfe[rm].re, Zfe[rm].im, dcr, dci, S, wr, wi);
-                st.S = f32e_from_fe(S);
-                st.wr = (float)wr;
-                st.wi = (float)wi;
-                refresh(st);
-            }
-            ++m;
-            ++iter;
-            ++rm;
-            if (per && rm == per) rm = 0;
-            Xc = orb[rm];
-            const float zr = Xc.x + st.s * st.wr, zi = Xc.y + st.s * st.wi;
-            const float zrad = zr * zr + zi * zi;
-            if (zrad > ESC2lo) {
-                double2 Xd = Zd[rm];
-                double sd = fe_to_double(fe_from_f32e(st.S));
-                double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
-                zrad_d = zdr * zdr + zdi * zdi;
-                if (zrad_d > g.ESC2) {
-                    outcome = 1;
-                    nesc = iter;
-                    break;
-                }
-            }
-            if (p.use_interior) {
-                if (conf_P > 0) {
-                    conf_D2 *= 4.0f * zrad;
-                    if (conf_D2 > 1e18f) conf_D2 = 1e18f;
-                    if (iter >= conf_next) {
-                        double2 Xd = Zd[rm];
-                        double sd = fe_to_double(fe_from_f32e(st.S));
-                        double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
-                        double qr = zdr - conf_zr, qi = zdi - conf_zi;
-                        if (qr * qr + qi * qi < p.interior_eps2 * (zdr * zdr + zdi * zdi) && conf_D2 < 1.0f) {
-                            if (++conf_count >= p.interior_confirm) {
-                                outcome = 2;
-                                break;
-                            }
-                            conf_zr = zdr;
-                            conf_zi = zdi;
-                            conf_D2 = 1.0f;
-                            conf_next = iter + conf_P;
-                        } else {
-                            conf_P = 0;
-                            ++conf_giveup;
-                        }
-                    }
-                } else if ((iter & 15) == 0 && conf_giveup < 3) {
-                    // FP32 screen: |dz - saved|^2 far above eps^2 |z|^2 cannot be a return.
-                    const float qr = zr - zsr_f, qi = zi - zsi_f;
-                    const bool maybe = qr * qr + qi * qi < 1e-11f * zrad;
-                    const bool save = iter - save_iter >= period_win;
-                    if (maybe || save) {
-                        double2 Xd = Zd[rm];
-                        double sd = fe_to_double(fe_from_f32e(st.S));
-                        double zdr = Xd.x + sd * (double)st.wr, zdi = Xd.y + sd * (double)st.wi;
-                        if (maybe) {
-                            double dqr = zdr - zsr, dqi = zdi - zsi;
-                            if (dqr * dqr + dqi * dqi < p.interior_eps2 * (zdr * zdr + zdi * zdi)) {
-                                conf_P = max(iter - save_iter, 1);
-                                conf_zr = zdr;
-                                conf_zi = zdi;
-                                conf_D2 = 1.0f;
-                                conf_next = iter + conf_P;
-                                conf_count = 0;
-                            }
-                        }
-                        if (save) {
-                            zsr = zdr;
-                            zsi = zdi;
-                            zsr_f = zr;
-                            zsi_f = zi;
-                            save_iter = iter;
-                            period_win += period_win;
-                        }
-                    }
-                }
-            }
-            // keep |w| ~ 1 (FP32-mantissa floatexp rescale)
-            const float wm2 = st.wr * st.wr + st.wi * st.wi;
-            if (wm2 > 1e16f || (wm2 < 1e-16f && wm2 > 0.0f)) {
-                const float wmag = sqrtf(wm2);
-                const float inv = 1.0f / wmag;
-                st.S = f32e_mulf(st.S, wmag);
-                st.wr *= inv;
-                st.wi *= inv;
-                refresh(st);
-            }
-            // Rebase: FP32 screen, FP64-floatexp decision (mp.cpp:3584-3615).
-            const float dzmag2 = st.s * st.s * (st.wr * st.wr + st.wi * st.wi);
-            if (zrad < 1e-8f || zrad < dzmag2 * 1.001f || (!per && m >= reflen)) {
-                const FE S = fe_from_f32e(st.S);
-                FE Xmr = Zfe[rm].re;
-                FE Xmi = Zfe[rm].im;
-                FE Swr = fe_mul_d(S, (double)st.wr), Swi = fe_mul_d(S, (double)st.wi);
-                FE zrfe = fe_add(Xmr, Swr), zife = fe_add(Xmi, Swi);
-                FE zradfe = fe_add(fe_mul(zrfe, zrfe), fe_mul(zife, zife));
-                FE dzfe = fe_add(fe_mul(Swr, Swr), fe_mul(Swi, Swi));
-                if ((!per && m >= reflen) || fe_abs_less(zradfe, dzfe)) {
-                    FE Snew = fe_sqrt(zradfe);
-                    if (Snew.m == 0.0) {
-                        st.wr = st.wi = 0.0f;
-                    } else {
-                        st.S = f32e_from_fe(Snew);
-                        st.wr = (float)fe_to_double(fe_div(zrfe, Snew));
-                        st.wi = (float)fe_to_double(fe_div(zife, Snew));
-                        refresh(st);
-                    }
-                    m = 0;
-                    rm = -1;
-                    Xc = make_float2(0.0f, 0.0f);
-                    ++n_rebase;
+        // Warp-synchronous refill: every idle lane takes a new sample together,
+        // so the per-sample setup runs once for all of them.
+        const unsigned idle = __ballot_sync(0xffffffffu, !live);
+        if (idle && !exhausted) {
+            int base = 0;
+            const int leader = __ffs(idle) - 1;
+            if ((int)lane_id == leader) base = (int)atomicAdd(&f.ctr->next, (unsigned)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base >= f.px.n) exhausted = true;
+            if (!live) {
+                const int i = base + __popc(idle & ((1u << lane_id) - 1u));
+                if (i < f.px.n && !stop) {
+                    lane_setup(L, i, f, p, dxf, dyf, orb);
+                    live = true;
                 }
             }
         }
-        if (outcome == 4) break;
-        if (outcome == 0) outcome = 2;
-        const int idx = (arr[0] * g.sub + g.sub / 2 + arr[2]) * g.W * g.sub + (arr[1] * g.sub + g.sub / 2 + arr[3]);
-        if (outcome == 1) {
-            f.out.iter[idx] = (float)((double)nesc - log(log(zrad_d) / 2.0 / kLn2m) / kLn2m);
-            if (f.out.escN) f.out.escN[idx] = nesc;
-            n_eff += (unsigned long long)nesc;
-        } else {
-            f.out.iter[idx] = -2.0f;
-            if (f.out.escN) f.out.escN[idx] = -1;
-            n_eff += (unsigned long long)g.mxit;
-            ++n_int;
+        if (__ballot_sync(0xffffffffu, live) == 0) break;
+        if (live) {
+            float zrad = 0.0f;
+            const int st = lane_run(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase);
+            if (st == 1) {
+                // smooth value N - log2(log2|z|) in FP32 (the output is FP32)
+                const float lg = log2f(zrad);
+                f.out.iter[L.oidx] = (float)L.iter - log2f(0.5f * lg);
+                if (f.out.escN) f.out.escN[L.oidx] = L.iter;
+                f.out.done[L.i] = 1;
+                n_eff += (unsigned long long)L.iter;
+                live = false;
+            } else if (st == 2) {
+                f.out.iter[L.oidx] = -2.0f;
+                if (f.out.escN) f.out.escN[L.oidx] = -1;
+                f.out.done[L.i] = 1;
+                n_eff += (unsigned long long)g.mxit;
+                ++n_int;
+                live = false;
+            }
         }
-        f.out.done[i] = 1;
+        if (((++rounds & 255u) == 0) && mcancelled(f)) {
+            stop = true;
+            exhausted = true;
+            live = false;
+        }
     }
     atomicAdd(&f.ctr->steps, n_steps);
     atomicAdd(&f.ctr->bla_applies, n_bla);
