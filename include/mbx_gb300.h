@@ -101,6 +101,23 @@ int mbx_abi_version(void);
  * the minibrot size estimate of nucleusSizeMag (mp.cpp:1195-1219) returned as
  * log10. Writes the nucleus as decimal strings (buf_len bytes each). Returns
  * the period, 0 when the disk holds no nucleus, or a negative MBX_E_* code. */
+/* Launch shape and numerics knobs of the mixed-precision pass. */
+typedef struct {
+    int threads;            /* block size: 128 or 256 */
+    int blocks_per_sm;      /* resident blocks per SM the kernel is compiled for: 2, 3 or 4 */
+    int smem_orbit_limit;   /* stage the FP32 orbit into shared memory when it fits in this many bytes (0: never) */
+    double rescale_window;  /* |w|^2 is kept in [1/window, window] */
+    double pass_ms;         /* autotune: GPU time of the calibration pass with this shape */
+} mbx_tuning;
+
+/* Sets the mixed-pass tuning of a context (values out of range are ignored). */
+int mbx_set_tuning(mbx_context* ctx, int threads, int blocks_per_sm, int smem_orbit_limit, double rescale_window);
+
+/* Autotuner: renders `calibration` (a floatexp frame) in mixed precision once
+ * per candidate (block size x resident blocks x orbit staging x rescale
+ * window), keeps the fastest shape on the context and returns it in *best. */
+int mbx_autotune(mbx_context* ctx, const mbx_request* calibration, mbx_tuning* best);
+
 /* Diagnostic: measured issue rate of dependent-free FMA chains on the context's
  * device, in TFLOP/s (an FMA counts as 2); fp64 = 1 for double, 0 for float.
  * The roofline denominators of the delta loops (FP64 / FP32 pipes). */

@@ -2,6 +2,7 @@
 // reference's CpuComputeBackend::valid (src/engine/compute_backend.cpp:263-272)
 // plus the engine's own constraints (odd sub, mp.cpp:230).
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <new>
 #include <string>
@@ -103,6 +104,71 @@ void mbx_reset_cancellation(mbx_context* c) {
 const char* mbx_info_name(const mbx_context* c) { return c ? c->name.c_str() : ""; }
 const char* mbx_info_detail(const mbx_context* c) { return c ? c->detail.c_str() : ""; }
 const char* mbx_last_error(const mbx_context* c) { return c ? c->last_error.c_str() : ""; }
+
+int mbx_set_tuning(mbx_context* c, int threads, int blocks_per_sm, int smem_orbit_limit, double rescale_window) {
+    if (!c) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    c->engine->set_tuning(threads, blocks_per_sm, smem_orbit_limit, (float)rescale_window);
+    return MBX_OK;
+}
+
+int mbx_autotune(mbx_context* c, const mbx_request* calib, mbx_tuning* best) {
+    if (!c || !calib) return MBX_E_INVALID;
+    std::string why;
+    if (validate(calib, why) != MBX_OK) {
+        c->last_error = why;
+        return MBX_E_INVALID;
+    }
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    std::lock_guard<std::mutex> g(g_gmp_mutex);
+    mbx_request r = *calib;
+    r.precision_mode = MBX_PRECISION_MIXED;
+    r.reuse_reference = 1;
+    mbx_stats st;
+    int rc = c->engine->compute(r, &st); // builds (and caches) the calibration reference
+    if (rc != MBX_OK) {
+        c->last_error = c->engine->error();
+        return rc;
+    }
+    if (!st.used_floatexp) {
+        c->last_error = "calibration frame does not use the floatexp path";
+        return MBX_E_INVALID;
+    }
+    const int threads_opts[] = {128, 256};
+    const int blocks_opts[] = {2, 3, 4};
+    const int smem_opts[] = {200 * 1024, 0};
+    const double window_opts[] = {1e8, 1e16, 1e30};
+    double best_ms = 1e300;
+    mbx_tuning b = {};
+    for (int t : threads_opts)
+        for (int bl : blocks_opts)
+            for (int sm : smem_opts)
+                for (double w : window_opts) {
+                    c->engine->set_tuning(t, bl, sm, (float)w);
+                    double ms = 1e300;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        rc = c->engine->compute(r, &st);
+                        if (rc != MBX_OK) {
+                            c->last_error = c->engine->error();
+                            return rc;
+                        }
+                        ms = std::min(ms, st.pass_gpu_ms);
+                    }
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        b.threads = t;
+                        b.blocks_per_sm = bl;
+                        b.smem_orbit_limit = sm;
+                        b.rescale_window = w;
+                        b.pass_ms = ms;
+                    }
+                }
+    c->engine->set_tuning(b.threads, b.blocks_per_sm, b.smem_orbit_limit, (float)b.rescale_window);
+    if (best) *best = b;
+    return MBX_OK;
+}
 
 int mbx_measure_fma_peak(mbx_context* c, int fp64, double* tflops) {
     if (!c || !tflops) return MBX_E_INVALID;

@@ -198,6 +198,23 @@ class Engine {
     int mixed_threads_ = 256;
     int mixed_blocks_per_sm_ = 2;
     int smem_orbit_limit_ = 200 * 1024;
+    float mixed_wmax2_ = 1e16f;
+
+  public:
+    void set_tuning(int threads, int blocks_per_sm, int smem_limit, float wmax2) {
+        if (threads == 128 || threads == 256) mixed_threads_ = threads;
+        if (blocks_per_sm >= 1 && blocks_per_sm <= 4) mixed_blocks_per_sm_ = blocks_per_sm;
+        if (smem_limit >= 0 && smem_limit <= 220 * 1024) smem_orbit_limit_ = smem_limit;
+        if (wmax2 >= 1e4f && wmax2 <= 1e30f) mixed_wmax2_ = wmax2;
+    }
+    void get_tuning(int* threads, int* blocks_per_sm, int* smem_limit, float* wmax2) const {
+        *threads = mixed_threads_;
+        *blocks_per_sm = mixed_blocks_per_sm_;
+        *smem_limit = smem_orbit_limit_;
+        *wmax2 = mixed_wmax2_;
+    }
+
+  private:
     float* out_iter_ = nullptr;
     float* out_norm_ = nullptr;
     int32_t* out_n_ = nullptr;

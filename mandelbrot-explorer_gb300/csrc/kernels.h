@@ -165,6 +165,7 @@ struct MixedParams {
     const uint8_t* Zsmall;   // 1 where |Z| is below FP32 normal range (use the floatexp shadow)
     int orbit_in_smem;       // stage the whole (periodic) orbit into shared memory
     int smem_entries;
+    float wmax2, wmin2;      // |w|^2 rescale window
 };
 cudaError_t launch_mixed_pass(const DeviceFrame& f, const MixedParams& p, int blocks, int threads, size_t smem, cudaStream_t st);
 

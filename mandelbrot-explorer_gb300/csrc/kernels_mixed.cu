@@ -503,9 +503,9 @@ __device__ int lane_run(Lane& L, int budget, const DeviceFrame& f, const MixedPa
                 }
             }
         }
-        // keep |w| ~ 1
+        // keep |w| ~ 1 (rescale window [1/wmax2, wmax2], autotuned)
         const float wm2 = L.wr * L.wr + L.wi * L.wi;
-        if (wm2 > 1e16f || (wm2 < 1e-16f && wm2 > 0.0f)) {
+        if (wm2 > p.wmax2 || (wm2 < p.wmin2 && wm2 > 0.0f)) {
             const float wmag = sqrtf(wm2), inv = 1.0f / wmag;
             L.S = f32e_mulf(L.S, wmag);
             L.wr *= inv;
@@ -524,7 +524,7 @@ __device__ int lane_run(Lane& L, int budget, const DeviceFrame& f, const MixedPa
             else {
                 const F32E z2 = f32e_norm(zrad, 0);
                 const float q = ldexpf_ftz(__fdividef(z2.m, dz2.m), max(-120, min(120, z2.e - dz2.e)));
-                if (q < 0.9999f) decide = (zrad > 1e-6f * (L.Xc.x * L.Xc.x + L.Xc.y * L.Xc.y) && L.s != 0.0f) ? 1 : 2;
+                if (q < 0.9999f) decide = (zrad > 0.25f * (L.Xc.x * L.Xc.x + L.Xc.y * L.Xc.y) && L.s != 0.0f) ? 1 : 2;
                 else if (q < 1.0001f) decide = 2;
             }
         }
@@ -563,7 +563,8 @@ __device__ int lane_run(Lane& L, int budget, const DeviceFrame& f, const MixedPa
     return 0;
 }
 
-__global__ void __launch_bounds__(256, 2) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e, const Bla32* bla32) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_mixed_pass(DeviceFrame f, MixedParams p, const int16_t* r2e, const Bla32* bla32) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ unsigned long long mbar;
     __shared__ int stage_ok;
@@ -755,13 +756,22 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
     const int threads = mixed_threads_;
     const int blocks = std::max(1, std::min((f.px.n + threads - 1) / threads, nsm_ * mixed_blocks_per_sm_));
     const size_t smem = p.orbit_in_smem ? bytes : 0;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_mixed_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    p.wmax2 = mixed_wmax2_;
+    p.wmin2 = 1.0f / mixed_wmax2_;
     DeviceFrame g = f;
     if (!(bla_.use && dr2e_.p)) g.bla.use = 0;
-    k_mixed_pass<<<blocks, threads, smem, st_>>>(g, p, dr2e_.p, mixed_bla32_ ? dbla32_.p : nullptr);
+    const Bla32* bt = mixed_bla32_ ? dbla32_.p : nullptr;
+    auto launch = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        kern<<<blocks, threads, smem, st_>>>(g, p, dr2e_.p, bt);
+        return cudaGetLastError();
+    };
+    if (mixed_blocks_per_sm_ >= 4) return launch(k_mixed_pass<4>);
+    if (mixed_blocks_per_sm_ == 3) return launch(k_mixed_pass<3>);
+    return launch(k_mixed_pass<2>);
     return cudaGetLastError();
 }
 

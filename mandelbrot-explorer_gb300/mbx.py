@@ -64,6 +64,19 @@ class _Request(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("threads", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int),
+        ("smem_orbit_limit", ctypes.c_int),
+        ("rescale_window", ctypes.c_double),
+        ("pass_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("total_ms", ctypes.c_double),
@@ -107,6 +120,8 @@ EXPORTS = (
     "mbx_abi_version",
     "mbx_find_nucleus",
     "mbx_measure_fma_peak",
+    "mbx_set_tuning",
+    "mbx_autotune",
 )
 
 _lib = None
@@ -141,6 +156,10 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_abi_version.restype = ctypes.c_int
         lib.mbx_measure_fma_peak.restype = ctypes.c_int
         lib.mbx_measure_fma_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.mbx_set_tuning.restype = ctypes.c_int
+        lib.mbx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        lib.mbx_autotune.restype = ctypes.c_int
+        lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
         lib.mbx_find_nucleus.restype = ctypes.c_int
         lib.mbx_find_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         if path is None:
@@ -255,7 +274,29 @@ class CudaComputeBackend:
             return buf.data_ptr(), True
         raise TypeError("output buffers must be numpy arrays or torch CUDA tensors")
 
+    def autotune(self, req: ComputeRequest) -> dict:
+        """Times the mixed pass over launch shapes on `req` and keeps the fastest."""
+        r, _keep = self._build(req)
+        t = Tuning()
+        rc = self._lib.mbx_autotune(self._ctx, ctypes.byref(r), ctypes.byref(t))
+        if rc != OK:
+            raise RuntimeError("autotune failed (%d): %s" % (rc, self.last_error()))
+        return t.as_dict()
+
+    def set_tuning(self, threads=256, blocks_per_sm=2, smem_orbit_limit=200 * 1024, rescale_window=1e16):
+        rc = self._lib.mbx_set_tuning(self._ctx, threads, blocks_per_sm, smem_orbit_limit, rescale_window)
+        if rc != OK:
+            raise RuntimeError("set_tuning failed (%d)" % rc)
+
     def compute_status(self, req: ComputeRequest) -> int:
+        r, _keep = self._build(req)
+        st = Stats()
+        rc = self._lib.mbx_compute(self._ctx, ctypes.byref(r), ctypes.byref(st))
+        self.last_stats = st
+        self.last_status = rc
+        return rc
+
+    def _build(self, req: ComputeRequest):
         n = req.sample_count()
         if req.iterations is None:
             req.iterations = np.empty(n, np.float32)
@@ -290,11 +331,7 @@ class CudaComputeBackend:
             ctypes.cast(ctypes.pointer(req.progress), ctypes.c_void_p) if req.progress is not None else None,
             1 if req.reuse_reference else 0,
         )
-        st = Stats()
-        rc = self._lib.mbx_compute(self._ctx, ctypes.byref(r), ctypes.byref(st))
-        self.last_stats = st
-        self.last_status = rc
-        return rc
+        return r, (req.iterations, req.normal, req.escape_iteration)
 
     def measure_fma_peak(self, fp64: bool) -> float:
         """Measured FMA issue rate of the device in TFLOP/s (FMA = 2 flops)."""
