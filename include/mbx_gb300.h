@@ -35,6 +35,7 @@ extern "C" {
 #define MBX_E_NODEVICE (-4)    /* no usable CUDA device (there is no CPU fallback) */
 #define MBX_E_BUSY (-5)        /* another compute is active on this context */
 #define MBX_E_NOMEM (-6)       /* device or host allocation failed */
+#define MBX_E_TOO_LARGE (-7)   /* frame exceeds a fixed capacity (mbx_render_shallow_noalloc) */
 
 typedef struct mbx_context mbx_context;
 
@@ -125,6 +126,27 @@ int mbx_measure_fma_peak(mbx_context* ctx, int fp64, double* tflops);
 
 int mbx_find_nucleus(const char* center_re, const char* center_im, const char* radius, int max_period, int precision_bits,
                      char* nucleus_re, char* nucleus_im, int buf_len, double* size_log10);
+
+/* Allocation-free render of a shallow frame (no reference counterpart: the
+ * reference has no device and allocates its buffers itself). For callers that
+ * cannot allocate device memory: the caller passes the frame geometry — the
+ * lower-left corner c0 and the pixel spacings dx, dy as doubles, i.e. the
+ * double values the reference derives at mp.cpp:1445-1448 — and device
+ * pointers to its own output buffers (iterations required; escape_iteration
+ * and normal optional; width*height entries). The direct-iteration pass
+ * (floatPointCompute semantics, mp.cpp:330-532) runs on `stream` (a
+ * cudaStream_t, NULL for the default stream) and the call returns after it
+ * completes. Its scratch (work counters, completion flags) is one fixed device
+ * array of 256 B + 2,097,152 B that every GPU loading this library holds until
+ * the process exits; frames above 2,097,152 samples are rejected with
+ * MBX_E_TOO_LARGE. The first call on each device resolves the array's device
+ * address with that device current, so make that first call before any stream
+ * capture. All calls share the one array: calls that overlap on the GPU race.
+ * Coloring bits: MBX_EXTERIOR_DIST_EST and MBX_DE_OVERLAY only (no
+ * supersampling). Calls no allocating CUDA or library routine. */
+int mbx_render_shallow_noalloc(double c0_re, double c0_im, double dx, double dy, int width, int height, int max_iterations,
+                               double bailout, int coloring_method, float* iterations, int32_t* escape_iteration,
+                               float* normal, void* stream);
 
 #ifdef __cplusplus
 }

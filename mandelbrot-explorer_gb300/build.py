@@ -34,6 +34,7 @@ def units():
     return [
         ("kernels_exact.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "kernels_exact.cu")]),
         ("kernels_mixed.o", [NVCC] + common_nv + ["-fmad=true", "-c", os.path.join(SRC, "kernels_mixed.cu")]),
+        ("noalloc.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "noalloc.cu")]),
         ("engine.o", cxx + ["-c", os.path.join(SRC, "engine.cpp")]),
         ("capi.o", cxx + ["-c", os.path.join(SRC, "capi.cpp")]),
     ]

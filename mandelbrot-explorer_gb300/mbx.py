@@ -37,7 +37,7 @@ EMPTYPIXEL = -10.0
 PRECISION_EXACT = 0
 PRECISION_MIXED = 1
 
-OK, E_INVALID, E_CUDA, E_CANCELLED, E_NODEVICE, E_BUSY, E_NOMEM = 0, -1, -2, -3, -4, -5, -6
+OK, E_INVALID, E_CUDA, E_CANCELLED, E_NODEVICE, E_BUSY, E_NOMEM, E_TOO_LARGE = 0, -1, -2, -3, -4, -5, -6, -7
 
 
 class _Request(ctypes.Structure):
@@ -120,6 +120,7 @@ EXPORTS = (
     "mbx_abi_version",
     "mbx_find_nucleus",
     "mbx_measure_fma_peak",
+    "mbx_render_shallow_noalloc",
     "mbx_set_tuning",
     "mbx_autotune",
 )
@@ -160,6 +161,8 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
         lib.mbx_autotune.restype = ctypes.c_int
         lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
+        lib.mbx_render_shallow_noalloc.restype = ctypes.c_int
+        lib.mbx_render_shallow_noalloc.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 4
         lib.mbx_find_nucleus.restype = ctypes.c_int
         lib.mbx_find_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         if path is None:
