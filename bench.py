@@ -117,6 +117,26 @@ def cpu_reference(views_list, sample_w, sample_h, threads):
     return eff / dt / 1e9, dt, eff
 
 
+def profile_run(args, vlist):
+    """A small, fixed launch sequence for profilers: each listed view rendered
+    warmup + steps times in the mixed form with the default launch shape and a
+    resident reference; prints one JSON line of per-view frame times."""
+    import mbx
+
+    out = {}
+    for v in vlist:
+        be = mbx.create_compute_backend("cuda")
+        times = []
+        for k in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            _, st = render(be, mbx, v, mbx.PRECISION_MIXED, reuse=True, width=args.width, height=args.height)
+            if k >= args.warmup:
+                times.append((time.perf_counter() - t) * 1e3)
+        out[v["label"]] = {"frame_ms": float(np.mean(times)), "pass_gpu_ms": st["pass_gpu_ms"], "fp64_reruns": st["fp64_reruns"], "steps": st["steps"], "bla_applies": st["bla_applies"]}
+        be.close()
+    print(json.dumps({"profile": out, "resolution": "%dx%d" % (args.width, args.height)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -128,6 +148,7 @@ def main():
     ap.add_argument("--cpu-sample", default="1920x1080", help="cpu_baseline sample size (same views); one render of each")
     ap.add_argument("--ref-sample", default="960x540", help="--impl reference per-step sample size (same views)")
     ap.add_argument("--plain-sample", default="480x270", help="plain FP64 GPU sample size (same views); 'full' for 1920x1080")
+    ap.add_argument("--profile", default=None, help="comma-separated view labels (e.g. 1e-300): render only those, default launch shape, no baselines (for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     import views
@@ -135,6 +156,10 @@ def main():
     vlist = views.c2_views(width=args.width, height=args.height)
     sw, sh = (int(x) for x in args.cpu_sample.split("x"))
     threads = os.cpu_count() or 1
+
+    if args.profile:
+        profile_run(args, [v for v in vlist if v["label"] in args.profile.split(",")])
+        return
 
     if args.impl == "reference":
         if rank != 0:
@@ -193,6 +218,7 @@ def main():
     W, H = args.width, args.height
     n = W * H
     outs = [(torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")) for _ in vlist]
+    reruns = {}
 
     def step(reuse=True):
         eff = steps = bla = launches = 0
@@ -207,6 +233,7 @@ def main():
             bla += st["bla_applies"]
             launches += st["kernel_launches"]
             gpu_ms += st["pass_gpu_ms"]
+            reruns[v["label"]] = st["fp64_reruns"]
         return eff, steps, bla, launches, gpu_ms, per_view
 
     # warm-up (the first step builds each frame's reference)
@@ -302,6 +329,7 @@ def main():
                 "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 16.6 MB written per frame; no flush",
                 "frame_ms": {v["label"]: float(ms / args.steps) for v, ms in zip(vlist, frame_ms)},
                 "autotuned": tuning,
+                "fp64_reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "frame_ms": e2e_t / len(vlist) * 1e3},
             "plain_fp64": {"value": plain_value, "unit": UNIT, "sample": "%dx%d" % (pw, ph), "frame_ms_scaled_to_1080p": plain_frame_ms},

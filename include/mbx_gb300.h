@@ -25,7 +25,7 @@ extern "C" {
 
 /* Arithmetic of the per-sample delta loop. */
 #define MBX_PRECISION_EXACT 0 /* FP64 / FP64-floatexp in the reference's exact operation order */
-#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration (floatexp frames only) */
+#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration (floatexp frames without DE colouring; others take the exact form) */
 
 /* Status codes (the reference returns bool + ComputeBackendInfo strings). */
 #define MBX_OK 0
@@ -75,6 +75,10 @@ typedef struct {
     double pass_gpu_ms;             /* CUDA-event time of the delta-pass kernels on the context's stream */
     int reused_reference;           /* 1 when the cached reference was reused */
     long long rebases;              /* rebases taken (mixed form) */
+    long long fp64_reruns;          /* mixed form: samples rerun in double-float (FP32 error estimate too large) */
+    double rerun_gpu_ms;            /* device time of the reruns (included in pass_gpu_ms) */
+    long long fp64_reruns_fp64;     /* of those, samples rerun again in FP64 (double-float estimate too large) */
+    double rerun_fp64_gpu_ms;       /* device time of the FP64 reruns (included in rerun_gpu_ms) */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns
@@ -96,12 +100,6 @@ const char* mbx_info_detail(const mbx_context* ctx);
 const char* mbx_last_error(const mbx_context* ctx);
 int mbx_abi_version(void);
 
-/* Host-only nucleus search (no context, no GPU): findNucleus for the disk
- * (centre, radius) — ball-arithmetic period up to max_period, then Newton
- * refinement (src/engine/mandel_perturbation.cpp:116-223, 1072-1107) — with
- * the minibrot size estimate of nucleusSizeMag (mp.cpp:1195-1219) returned as
- * log10. Writes the nucleus as decimal strings (buf_len bytes each). Returns
- * the period, 0 when the disk holds no nucleus, or a negative MBX_E_* code. */
 /* Launch shape and numerics knobs of the mixed-precision pass. */
 typedef struct {
     int threads;            /* block size: 128 or 256 */
@@ -124,8 +122,26 @@ int mbx_autotune(mbx_context* ctx, const mbx_request* calibration, mbx_tuning* b
  * The roofline denominators of the delta loops (FP64 / FP32 pipes). */
 int mbx_measure_fma_peak(mbx_context* ctx, int fp64, double* tflops);
 
+/* Host-only nucleus search (no context, no GPU): findNucleus for the disk
+ * (centre, radius) — ball-arithmetic period up to max_period, then Newton
+ * refinement (src/engine/mandel_perturbation.cpp:116-223, 1072-1107) — with
+ * the minibrot size estimate of nucleusSizeMag (mp.cpp:1195-1219) returned as
+ * log10. Writes the nucleus as decimal strings (buf_len bytes each). Returns
+ * the period, 0 when the disk holds no nucleus, or a negative MBX_E_* code. */
 int mbx_find_nucleus(const char* center_re, const char* center_im, const char* radius, int max_period, int precision_bits,
                      char* nucleus_re, char* nucleus_im, int buf_len, double* size_log10);
+
+/* Batched rendering of n (1..256) frames (no reference counterpart: the
+ * reference renders one frame per compute() call). Each frame is prepared as
+ * by mbx_compute (reference orbit, BLA tables, outputs); the probe and main
+ * passes of every frame in the mixed form (floatexp, no DE colouring, sub 1)
+ * then run in shared persistent launches — one batch-wide work counter over
+ * all frames' samples, then the double-float and FP64 rerun tiers — captured
+ * once as a CUDA graph and replayed while the batch keeps its shape. Other
+ * frames are rendered one by one. Results are identical to mbx_compute of
+ * each frame. view_stats (n entries) and batch_stats may be NULL; the shared
+ * passes' counters go to batch_stats. Frames need fewer than 65536 sample rows. */
+int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats);
 
 /* Allocation-free render of a shallow frame (no reference counterpart: the
  * reference has no device and allocates its buffers itself). For callers that

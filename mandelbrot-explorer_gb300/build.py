@@ -37,6 +37,7 @@ def units():
         ("noalloc.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "noalloc.cu")]),
         ("engine.o", cxx + ["-c", os.path.join(SRC, "engine.cpp")]),
         ("capi.o", cxx + ["-c", os.path.join(SRC, "capi.cpp")]),
+        ("batch.o", cxx + ["-c", os.path.join(SRC, "batch.cpp")]),
     ]
 
 

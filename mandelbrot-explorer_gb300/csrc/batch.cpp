@@ -1,0 +1,255 @@
+// Batched rendering (batch.h). The engines prepare their frames on their own
+// streams; the runner waits for them, uploads the view descriptors and replays
+// (or captures, when the shape changed) one CUDA graph holding every pass of
+// every view:
+//   memset counters -> probe: FP32, double-float, FP64 lane passes -> interior
+//   gate -> main: FP32, double-float, FP64 lane passes -> counters to the host.
+#include "batch.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace mbx {
+
+namespace {
+int cuda_fail(std::string& err, const char* what, cudaError_t e) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return MBX_E_CUDA;
+}
+} // namespace
+
+BatchRunner::~BatchRunner() {
+    if (st_) cudaStreamSynchronize(st_);
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    for (void* p : {(void*)d_probe_, (void*)d_main_, (void*)d_ctr_, (void*)d_view_interior_, (void*)d_qa_, (void*)d_qb_})
+        if (p) cudaFree(p);
+    if (h_desc_) cudaFreeHost(h_desc_);
+    if (h_ctr_) cudaFreeHost(h_ctr_);
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    if (st_) cudaStreamDestroy(st_);
+}
+
+void BatchRunner::cancel() {
+    for (auto& e : eng_) e->cancel();
+}
+void BatchRunner::reset_cancel() {
+    for (auto& e : eng_) e->reset_cancel();
+}
+
+int BatchRunner::ensure_engines(int n, std::string& err) {
+    if (!st_) {
+        if (cudaSetDevice(device_) != cudaSuccess || cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess) {
+            err = "batch stream creation failed";
+            return MBX_E_CUDA;
+        }
+    }
+    while ((int)eng_.size() < n) {
+        std::unique_ptr<Engine> e(new Engine(device_));
+        std::string why;
+        if (e->init(why) != 0) {
+            err = "batch engine initialisation failed: " + why;
+            return MBX_E_CUDA;
+        }
+        eng_.push_back(std::move(e));
+    }
+    return MBX_OK;
+}
+
+int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err) {
+    if (nviews > cap_views_) {
+        if (d_probe_) cudaFree(d_probe_);
+        if (d_main_) cudaFree(d_main_);
+        if (d_view_interior_) cudaFree(d_view_interior_);
+        if (h_desc_) cudaFreeHost(h_desc_);
+        d_probe_ = d_main_ = nullptr;
+        d_view_interior_ = nullptr;
+        h_desc_ = nullptr;
+        if (cudaMalloc(&d_probe_, sizeof(ViewDesc) * nviews) != cudaSuccess || cudaMalloc(&d_main_, sizeof(ViewDesc) * nviews) != cudaSuccess ||
+            cudaMalloc(&d_view_interior_, sizeof(unsigned) * nviews) != cudaSuccess ||
+            cudaHostAlloc((void**)&h_desc_, sizeof(ViewDesc) * 2 * nviews, cudaHostAllocDefault) != cudaSuccess) {
+            err = "batch descriptor allocation failed";
+            cap_views_ = 0;
+            return MBX_E_NOMEM;
+        }
+        cap_views_ = nviews;
+        g_views_ = -1; // the graph holds the old pointers
+    }
+    if (!d_ctr_) {
+        if (cudaMalloc(&d_ctr_, 6 * sizeof(Counters)) != cudaSuccess || cudaHostAlloc((void**)&h_ctr_, 6 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) {
+            err = "batch counter allocation failed";
+            return MBX_E_NOMEM;
+        }
+    }
+    if (capacity > cap_samples_) {
+        if (d_qa_) cudaFree(d_qa_);
+        if (d_qb_) cudaFree(d_qb_);
+        d_qa_ = d_qb_ = nullptr;
+        if (cudaMalloc(&d_qa_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&d_qb_, sizeof(uint64_t) * capacity) != cudaSuccess) {
+            err = "batch queue allocation failed";
+            cap_samples_ = 0;
+            return MBX_E_NOMEM;
+        }
+        cap_samples_ = capacity;
+        g_views_ = -1;
+    }
+    return MBX_OK;
+}
+
+int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, std::string& err) {
+    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag) return MBX_OK;
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+    int nsm = eng_[0]->sm_count();
+    cudaError_t e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
+    cudaMemsetAsync(d_ctr_, 0, 6 * sizeof(Counters), st_);
+    cudaMemsetAsync(d_view_interior_, 0, sizeof(unsigned) * nviews, st_);
+    auto tiers = [&](const ViewDesc* views, unsigned total, int c0, unsigned* vint) {
+        BatchArgs a{};
+        a.views = views;
+        a.nviews = nviews;
+        a.capacity = cap_samples_;
+        a.view_interior = vint;
+        a.cancel = cancel_flag;
+        // FP32 over all samples
+        a.total = total;
+        a.queue = nullptr;
+        a.queue_n = nullptr;
+        a.ctr = d_ctr_ + c0;
+        a.next_queue = d_qa_;
+        launch_batch_pass(0, a, nsm, st_);
+        // double-float over the FP32 pass's queue
+        a.queue = d_qa_;
+        a.queue_n = &d_ctr_[c0].rerun_n;
+        a.ctr = d_ctr_ + c0 + 1;
+        a.next_queue = d_qb_;
+        launch_batch_pass(1, a, nsm, st_);
+        // FP64 over the double-float pass's queue
+        a.queue = d_qb_;
+        a.queue_n = &d_ctr_[c0 + 1].rerun_n;
+        a.ctr = d_ctr_ + c0 + 2;
+        a.next_queue = nullptr;
+        launch_batch_pass(2, a, nsm, st_);
+    };
+    tiers(d_probe_, probe_total, 0, d_view_interior_);
+    launch_batch_gate(d_main_, nviews, d_view_interior_, st_);
+    tiers(d_main_, main_total, 3, nullptr);
+    cudaMemcpyAsync(h_ctr_, d_ctr_, 6 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    e = cudaStreamEndCapture(st_, &graph_);
+    if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
+    e = cudaGraphInstantiate(&exec_, graph_, 0);
+    if (e != cudaSuccess) return cuda_fail(err, "graph instantiation", e);
+    g_views_ = nviews;
+    g_probe_ = probe_total;
+    g_main_ = main_total;
+    g_cancel_ = cancel_flag;
+    return MBX_OK;
+}
+
+int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats, volatile int* cancel_flag, std::string& err) {
+    if (n < 1 || n > kBatchMaxViews) {
+        err = "batch size must be in [1, 256]";
+        return MBX_E_INVALID;
+    }
+    int rc = ensure_engines(n, err);
+    if (rc != MBX_OK) return rc;
+    std::vector<BatchSlot> slots(n);
+    std::vector<mbx_stats> vst(n);
+    for (int i = 0; i < n; ++i) {
+        rc = eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
+        if (rc != MBX_OK) {
+            err = eng_[i]->error();
+            return rc;
+        }
+    }
+    std::vector<int> deferred;
+    for (int i = 0; i < n; ++i)
+        if (slots[i].deferred) deferred.push_back(i);
+    mbx_stats bs = mbx_stats();
+    if (!deferred.empty()) {
+        const int nv = (int)deferred.size();
+        unsigned probe_total = 0, main_total = 0;
+        for (int k = 0; k < nv; ++k) {
+            const int i = deferred[k];
+            if (reqs[i].height * reqs[i].sub >= (1 << 16)) {
+                err = "batched frames must have fewer than 65536 sample rows";
+                return MBX_E_INVALID;
+            }
+            slots[i].probe.base = probe_total;
+            slots[i].main.base = main_total;
+            probe_total += slots[i].probe.count;
+            main_total += slots[i].main.count;
+        }
+        rc = ensure_buffers(nv, std::max(probe_total, main_total), err);
+        if (rc != MBX_OK) return rc;
+        for (int k = 0; k < nv; ++k) {
+            h_desc_[k] = slots[deferred[k]].probe;
+            h_desc_[nv + k] = slots[deferred[k]].main;
+        }
+        // the engines prepared their frames on their own streams
+        for (int k = 0; k < nv; ++k) {
+            cudaError_t e = cudaStreamSynchronize(eng_[deferred[k]]->stream());
+            if (e != cudaSuccess) return cuda_fail(err, "batch preparation", e);
+        }
+        cudaMemcpyAsync(d_probe_, h_desc_, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(d_main_, h_desc_ + nv, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
+        rc = build_graph(nv, probe_total, main_total, cancel_flag, err);
+        if (rc != MBX_OK) return rc;
+        cudaEventRecord(ev0_, st_);
+        cudaError_t e = cudaGraphLaunch(exec_, st_);
+        if (e != cudaSuccess) return cuda_fail(err, "graph launch", e);
+        cudaEventRecord(ev1_, st_);
+        e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return cuda_fail(err, "batched passes", e);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev0_, ev1_);
+        if (cancel_flag && *cancel_flag) {
+            err = "cancelled";
+            return MBX_E_CANCELLED;
+        }
+        bs.pass_gpu_ms = ms;
+        bs.kernel_launches = 7;
+        bs.passes = 2;
+        for (int c = 0; c < 6; ++c) {
+            const Counters& k = h_ctr_[c];
+            bs.steps += (long long)k.steps;
+            bs.bla_applies += (long long)k.bla_applies;
+            bs.bla_skipped += (long long)k.bla_skipped;
+            bs.effective_iterations += (long long)k.effective_iters;
+            bs.interior += (int)k.interior;
+            bs.rebases += (long long)k.rebases;
+        }
+        bs.fp64_reruns = (long long)h_ctr_[0].rerun_n + h_ctr_[3].rerun_n;
+        bs.fp64_reruns_fp64 = (long long)h_ctr_[1].rerun_n + h_ctr_[4].rerun_n;
+        bs.samples = (int)(probe_total + main_total);
+        const unsigned want[2] = {probe_total, main_total};
+        for (int ph = 0; ph < 2; ++ph) {
+            const Counters* c = h_ctr_ + 3 * ph;
+            // every sample finishes in the FP32 pass or one of the queues it feeds
+            if (c[0].finished != want[ph] || c[1].finished != std::min(c[0].rerun_n, cap_samples_) ||
+                c[2].finished != std::min(c[1].rerun_n, cap_samples_)) {
+                err = "batched pass left samples unfinished";
+                return MBX_E_CUDA;
+            }
+        }
+        for (int k = 0; k < nv; ++k) {
+            const int i = deferred[k];
+            rc = eng_[i]->batch_finish(reqs[i], &vst[i]);
+            if (rc != MBX_OK) {
+                err = eng_[i]->error();
+                return rc;
+            }
+        }
+    }
+    if (view_stats)
+        for (int i = 0; i < n; ++i) view_stats[i] = vst[i];
+    if (batch_stats) *batch_stats = bs;
+    return MBX_OK;
+}
+
+} // namespace mbx

@@ -1,0 +1,51 @@
+// Batched rendering of several views: one engine per view prepares its frame
+// (reference orbit, BLA tables, outputs), then one launch sequence runs the
+// probe and main passes of all views together — a batch-wide work counter
+// shared by the persistent lane passes, followed by the two rerun tiers — as a
+// CUDA graph that is replayed while the batch's shape stays the same.
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace mbx {
+
+class BatchRunner {
+  public:
+    explicit BatchRunner(int device) : device_(device) {}
+    ~BatchRunner();
+    // Renders reqs[0..n) (each validated by the caller). view_stats may be
+    // null; batch_stats (may be null) receives the shared passes' counters.
+    int run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats, volatile int* cancel_flag, std::string& err);
+    void cancel();
+    void reset_cancel();
+
+  private:
+    int ensure_engines(int n, std::string& err);
+    int ensure_buffers(int nviews, unsigned capacity, std::string& err);
+    int build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, std::string& err);
+
+    int device_;
+    std::vector<std::unique_ptr<Engine>> eng_;
+    cudaStream_t st_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    ViewDesc* d_probe_ = nullptr;
+    ViewDesc* d_main_ = nullptr;
+    ViewDesc* h_desc_ = nullptr;   // pinned staging: probe descriptors then main descriptors
+    Counters* d_ctr_ = nullptr;    // 6 blocks: probe FP32 / double-float / FP64, main likewise
+    Counters* h_ctr_ = nullptr;
+    unsigned* d_view_interior_ = nullptr;
+    uint64_t* d_qa_ = nullptr;     // FP32 -> double-float queue
+    uint64_t* d_qb_ = nullptr;     // double-float -> FP64 queue
+    int cap_views_ = 0;
+    unsigned cap_samples_ = 0;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int g_views_ = -1;
+    unsigned g_probe_ = 0, g_main_ = 0;
+    volatile int* g_cancel_ = nullptr;
+};
+
+} // namespace mbx

@@ -7,10 +7,12 @@
 #include <new>
 #include <string>
 
+#include "batch.h"
 #include "engine.h"
 
 struct mbx_context {
     mbx::Engine* engine = nullptr;
+    mbx::BatchRunner* batch = nullptr;
     std::string name = "cuda";
     std::string detail;
     std::string last_error;
@@ -73,8 +75,31 @@ mbx_context* mbx_create(int device, char* err, int err_len) {
 
 void mbx_destroy(mbx_context* c) {
     if (!c) return;
+    delete c->batch;
     delete c->engine;
     delete c;
+}
+
+int mbx_compute_batch(mbx_context* c, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats) {
+    if (!c || !reqs || n < 1 || n > mbx::kBatchMaxViews) return MBX_E_INVALID;
+    std::string why;
+    for (int i = 0; i < n; ++i) {
+        int v = validate(reqs + i, why);
+        if (v != MBX_OK) {
+            std::lock_guard<std::mutex> l(c->mu);
+            c->last_error = "request " + std::to_string(i) + ": " + why;
+            return v;
+        }
+    }
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    std::lock_guard<std::mutex> g(g_gmp_mutex);
+    if (!c->batch) c->batch = new (std::nothrow) mbx::BatchRunner(c->engine->device());
+    if (!c->batch) return MBX_E_NOMEM;
+    std::string err;
+    int rc = c->batch->run(reqs, n, view_stats, batch_stats, c->engine->device_cancel_flag(), err);
+    c->last_error = rc == MBX_OK ? std::string() : (err.empty() ? std::string("batch failed") : err);
+    return rc;
 }
 
 int mbx_compute(mbx_context* c, const mbx_request* r, mbx_stats* stats) {
@@ -97,9 +122,11 @@ int mbx_compute(mbx_context* c, const mbx_request* r, mbx_stats* stats) {
 
 void mbx_cancel(mbx_context* c) {
     if (c && c->engine) c->engine->cancel();
+    if (c && c->batch) c->batch->cancel();
 }
 void mbx_reset_cancellation(mbx_context* c) {
     if (c && c->engine) c->engine->reset_cancel();
+    if (c && c->batch) c->batch->reset_cancel();
 }
 const char* mbx_info_name(const mbx_context* c) { return c ? c->name.c_str() : ""; }
 const char* mbx_info_detail(const mbx_context* c) { return c ? c->detail.c_str() : ""; }

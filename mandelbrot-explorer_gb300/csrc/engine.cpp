@@ -242,9 +242,12 @@ int Engine::init(std::string& err) {
     nsm_ = prop.multiProcessorCount;
     snprintf(devname_, sizeof(devname_), "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor, nsm_);
     if (cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess) return -1;
-    if (cudaMalloc(&dctr_, sizeof(Counters)) != cudaSuccess) return -1;
-    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess) return -1;
-    if (cudaHostAlloc(&hctr_, sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) return -1;
+    // Counters of a pass, and of the two rerun passes that follow a mixed pass.
+    if (cudaMalloc(&dctr_, 3 * sizeof(Counters)) != cudaSuccess) return -1;
+    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess || cudaEventCreate(&evm_) != cudaSuccess ||
+        cudaEventCreate(&evd_) != cudaSuccess)
+        return -1;
+    if (cudaHostAlloc(&hctr_, 3 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) return -1;
     if (cudaHostAlloc((void**)&hcancel_, sizeof(int), cudaHostAllocMapped) != cudaSuccess) return -1;
     *hcancel_ = 0;
     if (cudaHostGetDevicePointer((void**)&dcancel_, (void*)hcancel_, 0) != cudaSuccess) return -1;
@@ -255,11 +258,14 @@ void Engine::release_device() {
     if (st_) cudaStreamSynchronize(st_);
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
-                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dr2e_.p, (void*)dbla32_.p})
+                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dbla64_.p,
+                    (void*)drerun_keys_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p})
         if (p) cudaFree(p);
     if (dctr_) cudaFree(dctr_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    if (evm_) cudaEventDestroy(evm_);
+    if (evd_) cudaEventDestroy(evd_);
     if (hctr_) cudaFreeHost(hctr_);
     if (hcancel_) cudaFreeHost((void*)hcancel_);
     if (st_) cudaStreamDestroy(st_);
@@ -1016,10 +1022,150 @@ FrameGeom Engine::geom() const {
     return g;
 }
 
+FeParams Engine::fe_params(int mx_ref_it) const {
+    FeParams p;
+    p.g = geom();
+    p.dxfe = dxfe_;
+    p.dyfe = dyfe_;
+    p.ref_x = ref_x_;
+    p.ref_y = ref_y_;
+    p.per = ref_period_;
+    p.mx_ref_it = mx_ref_it;
+    p.use_interior = use_interior_ ? 1 : 0;
+    p.int_rep = 1;
+    p.interior_confirm = interior_confirm_;
+    p.interior_eps2 = interior_eps2_;
+    p.fused = 1;
+    p.no_bla_kernel = (!use_bla_ && !deriv_) ? 1 : 0;
+    p.ref_period_gt0 = ref_period_ > 0 ? 1 : 0;
+    p.cutoff_sensitive = fe_cutoff_sensitive_ ? 1 : 0;
+    return p;
+}
+
+// Mixed-form pass over a pixel set, three lane passes on one stream with no
+// host round trip between them: the FP32 pass; the double-float pass over the
+// samples whose FP32 error estimate could change the result; the FP64 pass over
+// those the double-float estimate still cannot vouch for. Each rerun pass reads
+// its queue length on the device. The host then reads three counter blocks; it
+// scans flags only when a block left samples behind (orbit staging timed out).
+int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it) {
+    PixelSet px = grid;
+    int n = grid.n;
+    std::vector<uint64_t> kept;
+    if (keys) {
+        n = (int)keys->size();
+        if (n == 0) return MBX_OK;
+        if (!ensure(dkeys_, n)) return MBX_E_NOMEM;
+        cudaMemcpyAsync(dkeys_.p, keys->data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st_);
+        px.keys = dkeys_.p;
+        px.n = n;
+        kept.swap(*keys);
+    }
+    if (n <= 0) return MBX_OK;
+    if (!ensure(ddone_, n) || !ensure(drerun_keys_, n) || !ensure(drerun2_keys_, n) || !ensure(drerun_done_, n) || !ensure(drerun_gmp_, n))
+        return MBX_E_NOMEM;
+    cudaMemsetAsync(ddone_.p, 0, n, st_);
+    cudaMemsetAsync(dctr_, 0, 3 * sizeof(Counters), st_);
+    ++stats_.passes;
+    DeviceFrame f = frame_view();
+    f.px = px;
+    f.rerun_keys = drerun_keys_.p;
+    const double t0 = now_ms();
+    cudaEventRecord(ev0_, st_);
+    cudaError_t e = run_mixed_pass(f);
+    ++stats_.kernel_launches;
+    if (e != cudaSuccess) return fail_cuda("mixed pass launch", e);
+    cudaEventRecord(evm_, st_);
+    auto queue_frame = [&](uint64_t* q, int ctr_in, uint64_t* next_q, int ctr_out) {
+        DeviceFrame r = frame_view();
+        r.px = PixelSet();
+        r.px.keys = q;
+        r.px.n = n;
+        r.px.n_dev = &dctr_[ctr_in].rerun_n;
+        r.px.grid_w = r.px.grid_h = r.px.grid_step = 1;
+        r.px.skip_i = r.px.skip_j = -1;
+        r.out.done = drerun_done_.p;
+        r.out.gmp = drerun_gmp_.p;
+        r.ctr = dctr_ + ctr_out;
+        r.rerun_keys = next_q;
+        return r;
+    };
+    e = run_df_pass(queue_frame(drerun_keys_.p, 0, drerun2_keys_.p, 1));
+    ++stats_.kernel_launches;
+    if (e != cudaSuccess) return fail_cuda("double-float rerun launch", e);
+    cudaEventRecord(evd_, st_);
+    e = run_rerun_pass(queue_frame(drerun2_keys_.p, 1, nullptr, 2));
+    ++stats_.kernel_launches;
+    if (e != cudaSuccess) return fail_cuda("FP64 rerun launch", e);
+    cudaEventRecord(ev1_, st_);
+    cudaMemcpyAsync(hctr_, dctr_, 3 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    e = cudaStreamSynchronize(st_);
+    stats_.kernel_ms += now_ms() - t0;
+    if (e != cudaSuccess) return fail_cuda("mixed pass", e);
+    {
+        float ms = 0.0f, rms = 0.0f, fms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) stats_.pass_gpu_ms += ms;
+        if (cudaEventElapsedTime(&rms, evm_, ev1_) == cudaSuccess) stats_.rerun_gpu_ms += rms;
+        if (cudaEventElapsedTime(&fms, evd_, ev1_) == cudaSuccess) stats_.rerun_fp64_gpu_ms += fms;
+    }
+    if (cancel_.load()) return MBX_E_CANCELLED;
+    Counters& a = hctr_[0];
+    for (int k = 1; k < 3; ++k) {
+        const Counters& b = hctr_[k];
+        a.steps += b.steps;
+        a.bla_applies += b.bla_applies;
+        a.bla_skipped += b.bla_skipped;
+        a.effective_iters += b.effective_iters;
+        a.interior += b.interior; // callers read the pass's interior count from hctr_
+    }
+    stats_.rebases += (long long)a.rebases;
+    stats_.steps += (long long)a.steps;
+    stats_.bla_applies += (long long)a.bla_applies;
+    stats_.bla_skipped += (long long)a.bla_skipped;
+    stats_.effective_iterations += (long long)a.effective_iters;
+    stats_.interior += (int)a.interior;
+    stats_.fp64_reruns += std::min<unsigned>(a.rerun_n, (unsigned)n);
+    stats_.fp64_reruns_fp64 += std::min<unsigned>(hctr_[1].rerun_n, (unsigned)n);
+    stats_.samples += n;
+    if ((int)a.finished < n) {
+        // A block left samples unstarted (orbit staging timed out): scan the
+        // flags and take them through the FP64 floatexp pass.
+        hdone_.resize(n);
+        cudaMemcpyAsync(hdone_.data(), ddone_.p, n, cudaMemcpyDeviceToHost, st_);
+        e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return fail_cuda("pass readback", e);
+        std::vector<uint64_t> pending;
+        for (int i = 0; i < n; ++i) {
+            if (hdone_[i]) continue;
+            int arr[4];
+            if (keys) key_unpack(kept[i], arr);
+            else entry_coords(px, i, arr);
+            pending.push_back(key_pack(arr[0], arr[1], arr[2], arr[3]));
+        }
+        stats_.fp64_reruns += (long long)pending.size();
+        exact_rerun_ = true;
+        PixelSet g = PixelSet();
+        g.grid_w = g.grid_h = g.grid_step = 1;
+        g.skip_i = g.skip_j = -1;
+        const int rc = run_pass(&pending, g, mx_ref_it, nullptr, nullptr);
+        exact_rerun_ = false;
+        if (rc != MBX_OK) return rc;
+        if (!pending.empty()) {
+            err_ = "floatexp pass left samples unfinished";
+            return MBX_E_CUDA;
+        }
+    }
+    return MBX_OK;
+}
+
 // One delta pass over a pixel set (stepParallel, mp.cpp:2092-2607). On return
 // `keys` (if any) holds the still-pending entries in order and `new_ref` the
 // minimum-glitch-score entry (first in set order on ties), if any.
 int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it, bool* have_new_ref, int* new_ref) {
+    if (use_floatexp_ && mixed_active() && !exact_rerun_) {
+        if (have_new_ref) *have_new_ref = false;
+        return run_pass_mixed(keys, grid, mx_ref_it);
+    }
     PixelSet px = grid;
     int n = grid.n;
     if (keys) {
@@ -1043,25 +1189,8 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     const double t0 = now_ms();
     cudaError_t e;
     cudaEventRecord(ev0_, st_);
-    if (use_floatexp_ && mode_ == MBX_PRECISION_MIXED) {
-        e = run_mixed_pass(f);
-    } else if (use_floatexp_) {
-        FeParams p;
-        p.g = geom();
-        p.dxfe = dxfe_;
-        p.dyfe = dyfe_;
-        p.ref_x = ref_x_;
-        p.ref_y = ref_y_;
-        p.per = ref_period_;
-        p.mx_ref_it = mx_ref_it;
-        p.use_interior = use_interior_ ? 1 : 0;
-        p.int_rep = 1;
-        p.interior_confirm = interior_confirm_;
-        p.interior_eps2 = interior_eps2_;
-        p.fused = 1;
-        p.no_bla_kernel = (!use_bla_ && !deriv_) ? 1 : 0;
-        p.ref_period_gt0 = ref_period_ > 0 ? 1 : 0;
-        p.cutoff_sensitive = fe_cutoff_sensitive_ ? 1 : 0;
+    if (use_floatexp_) {
+        const FeParams p = fe_params(mx_ref_it);
         int blocks = std::min((n + threads - 1) / threads, nsm_ * 8);
         e = launch_fe_pass(f, p, blocks, threads, st_);
     } else {
@@ -1099,7 +1228,10 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     if (e != cudaSuccess) return fail_cuda("delta pass", e);
     {
         float ms = 0.0f;
-        if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) stats_.pass_gpu_ms += ms;
+        if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) {
+            stats_.pass_gpu_ms += ms;
+            if (exact_rerun_) stats_.rerun_gpu_ms += ms;
+        }
     }
     stats_.rebases += (long long)hctr_->rebases;
     if (cancel_.load()) return MBX_E_CANCELLED;
@@ -1226,6 +1358,74 @@ int Engine::flush_ref_value() {
 
 // ---------------------------------------------------------------------------
 // Mandel::Compute (mp.cpp:1388-2028) for the Mandelbrot mode.
+void Engine::fill_batch_slot() {
+    ViewDesc d{};
+    d.f = frame_view();
+    if (!(bla_.use && dbla32_.p)) d.f.bla.use = 0;
+    d.p = mixed_params();
+    d.bla32 = dbla32_.p;
+    d.orb32 = dZf_.p;
+    d.bladf = dbladf_.p;
+    d.orbdf = dZdf_.p;
+    d.bla64 = dbla64_.p;
+    d.orb64 = dZ_.p;
+    d.interior_gate = 0;
+    d.base = 0;
+    // probe on the 1/8 grid with interior detection on (mp.cpp:1668-1720)
+    ViewDesc pr = d;
+    pr.f.px = PixelSet();
+    pr.f.px.keys = nullptr;
+    pr.f.px.grid_w = W_;
+    pr.f.px.grid_h = H_;
+    pr.f.px.grid_step = 8;
+    pr.f.px.skip_i = pr.f.px.skip_j = -1;
+    pr.f.px.n = ((H_ + 7) / 8) * ((W_ + 7) / 8);
+    pr.p.use_interior = 1;
+    pr.count = (unsigned)pr.f.px.n;
+    // main pass over the frame minus the reference pixel
+    ViewDesc mn = d;
+    mn.f.px = PixelSet();
+    mn.f.px.keys = nullptr;
+    mn.f.px.grid_w = W_;
+    mn.f.px.grid_h = H_;
+    mn.f.px.grid_step = 1;
+    mn.f.px.skip_i = ref_virtual_ ? -1 : H_ / 2;
+    mn.f.px.skip_j = ref_virtual_ ? -1 : W_ / 2;
+    mn.f.px.n = W_ * H_ - (ref_virtual_ ? 0 : 1);
+    mn.p.use_interior = 1;
+    mn.interior_gate = 1;
+    mn.count = (unsigned)mn.f.px.n;
+    batch_slot_->probe = pr;
+    batch_slot_->main = mn;
+    batch_slot_->deferred = true;
+    stats_.passes += 2;
+    stats_.samples += pr.count + mn.count;
+}
+
+int Engine::compute_deferred(const mbx_request& r, BatchSlot* slot, mbx_stats* out_stats) {
+    slot->deferred = false;
+    batch_slot_ = slot;
+    const int rc = compute(r, out_stats);
+    batch_slot_ = nullptr;
+    return rc;
+}
+
+int Engine::batch_finish(const mbx_request& r, mbx_stats* out_stats) {
+    const size_t nsamp = (size_t)r.width * r.height * r.sub * r.sub;
+    const double t0 = now_ms();
+    if (!r.outputs_on_device) {
+        cudaMemcpyAsync(r.iterations, out_iter_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
+        if (r.normal) cudaMemcpyAsync(r.normal, out_norm_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
+        if (r.escape_iteration) cudaMemcpyAsync(r.escape_iteration, out_n_, sizeof(int32_t) * nsamp, cudaMemcpyDeviceToHost, st_);
+        cudaError_t e = cudaStreamSynchronize(st_);
+        stats_.copy_ms += now_ms() - t0;
+        if (e != cudaSuccess) return fail_cuda("output readback", e);
+    }
+    if (r.progress) *r.progress = 1.0f;
+    if (out_stats) *out_stats = stats_;
+    return MBX_OK;
+}
+
 int Engine::compute(const mbx_request& r, mbx_stats* out_stats) {
     bool expected = false;
     if (!active_.compare_exchange_strong(expected, true)) return MBX_E_BUSY;
@@ -1311,6 +1511,7 @@ int Engine::compute_frame(const mbx_request& r) {
     hD_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
     hZfe_.assign((size_t)MXIT_ + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
     int rc = render(cre, cim, msc, full_h, row_base, r.progress);
+    if (batch_slot_ && batch_slot_->deferred) return rc; // passes and readback follow in the batch
     if (rc == MBX_OK && !r.outputs_on_device) {
         const double t0 = now_ms();
         cudaMemcpyAsync(r.iterations, out_iter, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
@@ -1379,7 +1580,7 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
             rc = build_dc_tables();
             if (rc != MBX_OK) return rc;
         }
-        if (mode_ == MBX_PRECISION_MIXED && use_floatexp_) {
+        if (mixed_active() && use_floatexp_) {
             rc = prepare_mixed();
             if (rc != MBX_OK) return rc;
         }
@@ -1389,6 +1590,10 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     rc = flush_ref_value();
     if (rc != MBX_OK) return rc;
     if (progress) *progress = 0.08f;
+    if (batch_slot_ && use_floatexp_ && mixed_active() && SUB_ == 1) {
+        fill_batch_slot(); // the probe and main passes run in the batch's launches
+        return MBX_OK;
+    }
     // Interior auto-gate probe on the 1/8 grid (mp.cpp:1668-1720).
     {
         PixelSet g;

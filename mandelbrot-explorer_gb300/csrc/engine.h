@@ -69,6 +69,14 @@ int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_
 bool newton_nucleus(mpf_ptr cr, mpf_ptr ci, int period, mp_bitcnt_t prec, int maxit);
 int find_nucleus_disk(const char* cre, const char* cim, const char* radius, int maxp, int prec, std::string& nre, std::string& nim, double* size_log10);
 
+// A frame handed to a batch: the engine prepares everything up to the passes
+// (reference, BLA, outputs) and describes its probe and main pass; the batch
+// runs those passes for all its frames in shared launches.
+struct BatchSlot {
+    bool deferred = false;
+    ViewDesc probe, main;
+};
+
 class Engine {
   public:
     explicit Engine(int device);
@@ -79,6 +87,15 @@ class Engine {
     void reset_cancel();
     const std::string& error() const { return err_; }
     const char* device_name() const { return devname_; }
+    // Batch support: compute up to the passes (slot->deferred), or the whole
+    // frame when it is not eligible (mixed form, floatexp, no DE, sub 1);
+    // finish copies host outputs and completes the stats of a deferred frame.
+    int compute_deferred(const mbx_request& r, BatchSlot* slot, mbx_stats* st);
+    int batch_finish(const mbx_request& r, mbx_stats* st);
+    cudaStream_t stream() const { return st_; }
+    volatile int* device_cancel_flag() const { return dcancel_; }
+    int sm_count() const { return nsm_; }
+    int device() const { return device_; }
 
   private:
     int compute_frame(const mbx_request& r);
@@ -88,7 +105,12 @@ class Engine {
     int glitch_loop(std::vector<uint64_t>& pending, int& ref_it, bool have, int* nr, volatile float* progress);
     int supersample(int ref_it);
     int run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it, bool* have_new_ref, int* new_ref);
+    int run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it);
+    FeParams fe_params(int mx_ref_it) const;
     cudaError_t run_mixed_pass(const DeviceFrame& f);
+    cudaError_t run_rerun_pass(const DeviceFrame& f);
+    cudaError_t run_df_pass(const DeviceFrame& f);
+    MixedParams mixed_params() const;
     int prepare_mixed();
     int recompute_gmp(const std::vector<int>& list, const std::function<void(int, int*)>& key_of);
     int write_sample(const int* a, float v, int32_t n);
@@ -190,9 +212,18 @@ class Engine {
     DevBuf<uint64_t> dkeys_;
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
-    DevBuf<int16_t> dr2e_;
     DevBuf<Bla32> dbla32_;
-    bool mixed_bla32_ = true;
+    DevBuf<Bla64> dbla64_;
+    DevBuf<BlaDF> dbladf_;
+    DevBuf<df2> dZdf_;
+    DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
+    DevBuf<uint64_t> drerun2_keys_;           // double-float pass: queue for the FP64 pass
+    DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position
+    bool exact_rerun_ = false; // mixed form: the FP64 floatexp rerun of flagged samples is running
+    BatchSlot* batch_slot_ = nullptr;
+    void fill_batch_slot();
+    // The FP32 pass carries no derivative: DE colourings take the exact form.
+    bool mixed_active() const { return mode_ == MBX_PRECISION_MIXED && !deriv_; }
 
     // mixed-pass launch shape (set by the autotuner / defaults)
     int mixed_threads_ = 256;
@@ -235,7 +266,7 @@ class Engine {
     std::string frame_key_;
     bool reuse_ = false;
     int refs_built_in_frame_ = 0;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evm_ = nullptr, evd_ = nullptr;
     void save_cache(int ref_it);
     bool restore_cache(int* ref_it);
 

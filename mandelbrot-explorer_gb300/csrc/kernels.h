@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.cuh"
 #include "floatexp.h"
 
 namespace mbx {
@@ -30,14 +31,20 @@ struct FE2 {
     FE re, im;
 };
 
-// FP32-floatexp copy of one BLA entry for the mixed-precision pass: A and B as
-// float2 mantissas with one exponent each, radius^2 as mantissa + exponent.
-struct Bla32 {
-    float4 ab; // A.re, A.im (scaled by 2^-ea), B.re, B.im (scaled by 2^-eb)
+// Floatexp copy of one BLA entry for the lane passes (T = float: the mixed
+// pass, T = df32: the double-float rerun pass, T = double: the FP64 rerun
+// pass): A and B as mantissa pairs with one exponent each, radius^2 as mantissa
+// + exponent.
+template <class T>
+struct __align__(16) BlaEntry {
+    T ar, ai, br, bi; // A.re, A.im (scaled by 2^-ea), B.re, B.im (scaled by 2^-eb)
     int ea, eb;
-    float r2m; // r2 = r2m * 2^r2e, r2m in [0.5,1); 0 when r2 <= 0
+    T r2m;            // r2 = r2m * 2^r2e, r2m in [0.5,1); 0 when r2 <= 0
     int r2e;
 };
+using Bla32 = BlaEntry<float>;
+using BlaDF = BlaEntry<df32>;
+using Bla64 = BlaEntry<double>;
 
 // Reference orbit shadows in device memory (mp.h:295-371).
 struct OrbitView {
@@ -67,7 +74,28 @@ struct PixelSet {
     int n;
     int grid_w, grid_step, grid_h;
     int skip_i, skip_j;   // grid mode: pixel excluded (reference pixel), -1 none
+    const unsigned int* n_dev = nullptr; // list mode: entry count read on the device (bounded by n)
 };
+
+// Sample coordinates {row, col, subrow, subcol} of pass entry i.
+__host__ __device__ inline void entry_coords(const PixelSet& px, int i, int* a) {
+    if (px.keys) {
+        key_unpack(px.keys[i], a);
+        return;
+    }
+    // Grid mode: row-major over a strided grid, optionally skipping one pixel
+    // (the reference pixel, erased from the pending set at mp.cpp:1726).
+    int cols = (px.grid_w + px.grid_step - 1) / px.grid_step;
+    int q = i;
+    if (px.skip_i >= 0) {
+        int sq = (px.skip_i / px.grid_step) * cols + px.skip_j / px.grid_step;
+        if (q >= sq) ++q;
+    }
+    a[0] = (q / cols) * px.grid_step;
+    a[1] = (q % cols) * px.grid_step;
+    a[2] = 0;
+    a[3] = 0;
+}
 
 struct Outputs {
     float* iter;     // (W*sub) x (H*sub), reference layout (getIndex mp.cpp:4334-4340)
@@ -84,6 +112,9 @@ struct Counters {
     unsigned int interior;
     unsigned long long glitch_min_bits;  // min glitch score (as non-negative double bits)
     unsigned long long effective_iters;  // sum of N (maxiter for interior)
+    unsigned int rerun_n;                // mixed pass: entries queued for the FP64 floatexp pass
+    unsigned int finished;               // mixed pass: entries finished or queued
+    unsigned int gmp_flags;              // floatexp pass: entries flagged for the arbitrary-precision recompute
 };
 
 struct FrameGeom {
@@ -139,6 +170,7 @@ struct DeviceFrame {
     Outputs out;
     Counters* ctr;
     volatile int* cancel;    // host-mapped flag
+    uint64_t* rerun_keys = nullptr; // mixed pass: queue of sample keys for the FP64 floatexp pass
 };
 
 // Launchers (kernels_exact.cu).
@@ -167,6 +199,43 @@ struct MixedParams {
     int smem_entries;
     float wmax2, wmin2;      // |w|^2 rescale window
 };
-cudaError_t launch_mixed_pass(const DeviceFrame& f, const MixedParams& p, int blocks, int threads, size_t smem, cudaStream_t st);
+// The lane passes are launched by Engine::run_mixed_pass / run_df_pass /
+// run_rerun_pass (kernels_mixed.cu), which own their per-reference tables.
+
+// One view of a batch: what a lane needs to iterate that view's samples. The
+// batch passes read it from device memory per lane, so lanes of one warp may
+// work on different views.
+struct ViewDesc {
+    DeviceFrame f;           // outputs, orbit shadows, BLA view, the view's pixel set
+    MixedParams p;
+    const Bla32* bla32;
+    const float2* orb32;
+    const BlaDF* bladf;
+    const df2* orbdf;
+    const Bla64* bla64;
+    const double2* orb64;
+    unsigned base;           // first batch-wide sample index of this view
+    unsigned count;          // samples of this view in the pass
+    int interior_gate;       // main pass: interior detection follows the probe's interior count
+};
+
+// Batch-wide pass arguments. Queue entries are sample keys with the view index
+// in bits 56..63 (rows below 2^16).
+struct BatchArgs {
+    const ViewDesc* views;
+    int nviews;
+    unsigned total;          // sample count (FP32 pass)
+    const uint64_t* queue;   // rerun passes: queue of keys; null for the FP32 pass
+    const unsigned* queue_n; // its length (on the device)
+    unsigned capacity;       // queue capacity
+    Counters* ctr;           // work counter and totals of this pass
+    uint64_t* next_queue;    // where samples this pass cannot vouch for go (null: none)
+    unsigned* view_interior; // probe pass: interior count per view (null otherwise)
+    volatile int* cancel;
+};
+constexpr int kBatchViewShift = 56;
+constexpr int kBatchMaxViews = 256;
+cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st); // tier 0 FP32, 1 double-float, 2 FP64
+cudaError_t launch_batch_gate(ViewDesc* views, int n, const unsigned* view_interior, cudaStream_t st);
 
 } // namespace mbx

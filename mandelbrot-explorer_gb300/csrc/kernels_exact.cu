@@ -18,24 +18,7 @@ __device__ __forceinline__ int sample_index(const FrameGeom& g, const int* a) { 
 }
 
 // Resolve list entry `i` of the pass to its {row, col, subrow, subcol}.
-__device__ __forceinline__ void entry_key(const PixelSet& px, int i, int* a) {
-    if (px.keys) {
-        key_unpack(px.keys[i], a);
-        return;
-    }
-    // Grid mode: row-major over a strided grid, optionally skipping one pixel
-    // (the reference pixel, erased from the pending set at mp.cpp:1726).
-    int cols = (px.grid_w + px.grid_step - 1) / px.grid_step;
-    int q = i;
-    if (px.skip_i >= 0) {
-        int sq = (px.skip_i / px.grid_step) * cols + px.skip_j / px.grid_step;
-        if (q >= sq) ++q;
-    }
-    a[0] = (q / cols) * px.grid_step;
-    a[1] = (q % cols) * px.grid_step;
-    a[2] = 0;
-    a[3] = 0;
-}
+__device__ __forceinline__ void entry_key(const PixelSet& px, int i, int* a) { entry_coords(px, i, a); }
 
 __device__ __forceinline__ bool cancelled(const DeviceFrame& f) { return f.cancel && *f.cancel; }
 
@@ -845,10 +828,13 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
     const FrameGeom& g = p.g;
     unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0;
     unsigned int n_int = 0;
+    const int n = f.px.n_dev ? min((int)*f.px.n_dev, f.px.n) : f.px.n;
     for (;;) {
         if (cancelled(f)) break;
+        // plain read first: threads past the end leave without an atomic
+        if ((int)*(volatile unsigned int*)&f.ctr->next >= n) break;
         int i = (int)atomicAdd(&f.ctr->next, 1u);
-        if (i >= f.px.n) break;
+        if (i >= n) break;
         int arr[4];
         entry_key(f.px, i, arr);
         // dc in floatexp (mp.cpp:2160-2163).
@@ -862,7 +848,10 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
         // mp.cpp:2173-2183: EMPTY or cutoff-sensitive results go to the
         // arbitrary-precision recompute, flagged here for the host.
         const float v = o.value;
-        if (v == kEmpty || (p.cutoff_sensitive && (v < 0 || v > g.mxit - 16))) f.out.gmp[i] = 1;
+        if (v == kEmpty || (p.cutoff_sensitive && (v < 0 || v > g.mxit - 16))) {
+            f.out.gmp[i] = 1;
+            atomicAdd(&f.ctr->gmp_flags, 1u);
+        }
         f.out.iter[idx] = v;
         if (g.deovl && f.out.normal) f.out.normal[idx] = o.nrm;
         if (f.out.escN) f.out.escN[idx] = o.state == 1 ? o.n : -1;

@@ -1,0 +1,731 @@
+// Per-sample logic of the lane passes: floatexp helpers with a T mantissa
+// (float or double), the exact floatexp step, the floatexp BLA skip and the
+// lane state machine (setup, iterate, escape / interior / rebase decisions).
+//
+// Two instantiations run on the device (kernels_mixed.cu):
+//   * T = float: the mixed-precision pass. A running error estimate decides
+//     which FP32 results it may keep; it queues the other samples for
+//   * T = double: the FP64 rerun pass, the same lane in double precision, which
+//     costs ~15 FP64 operations per step (the reference-exact floatexp kernel
+//     spends several times that on floatexp bookkeeping).
+// Host-and-device code: the same source compiles as plain C++ so a host build
+// can step one sample for inspection. Semantics follow the reference's
+// rescaled loop (src/engine/mandel_perturbation.cpp:3287-3618, "mp.cpp").
+#pragma once
+#include <math.h>
+#include <string.h>
+
+#include "dfloat.cuh"
+#include "kernels.h"
+
+#ifdef __CUDACC__
+#define MBX_HDF __host__ __device__
+#else
+#define MBX_HDF inline
+#endif
+
+namespace mbx {
+
+MBX_HD unsigned fbits(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    unsigned u;
+    memcpy(&u, &x, 4);
+    return u;
+#endif
+}
+MBX_HD float bitsf(unsigned u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float x;
+    memcpy(&x, &u, 4);
+    return x;
+#endif
+}
+// a / b where a relative error of a few ulp is acceptable (screens only).
+MBX_HD float fdiv_approx(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdividef(a, b);
+#else
+    return a / b;
+#endif
+}
+MBX_HD double fdiv_approx(double a, double b) { return a / b; }
+MBX_HD float tsqrt(float x) { return sqrtf(x); }
+MBX_HD double tsqrt(double x) { return sqrt(x); }
+MBX_HD float tabs(float x) { return fabsf(x); }
+MBX_HD double tabs(double x) { return fabs(x); }
+MBX_HD float tmin(float a, float b) { return fminf(a, b); }
+MBX_HD double tmin(double a, double b) { return fmin(a, b); }
+// Position of the least significant set bit, 1-based; 0 for x == 0.
+MBX_HD int ffs32(int x) {
+#ifdef __CUDA_ARCH__
+    return __ffs(x);
+#else
+    return __builtin_ffs(x);
+#endif
+}
+MBX_HD int imax(int a, int b) { return a > b ? a : b; }
+MBX_HD int imin(int a, int b) { return a < b ? a : b; }
+MBX_HD int64_t lmax(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// ---- floatexp with a T mantissa: m in [0.5,1) (or 0), e int ---------------
+template <class T>
+struct TE {
+    T m;
+    int e;
+};
+using F32E = TE<float>;
+using F64E = TE<double>;
+
+MBX_HD F32E te_norm(float m, int e) {
+    if (m == 0.0f) return F32E{0.0f, 0};
+    unsigned b = fbits(m);
+    int ex = (int)((b >> 23) & 0xff);
+    if (ex == 0) { // subnormal mantissa: scale up exactly
+        m *= 16777216.0f;
+        b = fbits(m);
+        ex = (int)((b >> 23) & 0xff) - 24;
+    }
+    return F32E{bitsf((b & 0x807fffffu) | (126u << 23)), e + ex - 126};
+}
+MBX_HD F64E te_norm(double m, int e) {
+    if (m == 0.0) return F64E{0.0, 0};
+    uint64_t b = dbits(m);
+    int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0) {
+        m *= 18014398509481984.0; // 2^54, exact
+        b = dbits(m);
+        ex = (int)((b >> 52) & 0x7ff) - 54;
+    }
+    return F64E{bitsd((b & 0x800fffffffffffffull) | (1022ull << 52)), e + ex - 1022};
+}
+// a * 2^k for a normal (or zero) a, flushing below the type's normal range to
+// zero and saturating above it.
+MBX_HD float ldexp_ftz(float a, int k) {
+    if (a == 0.0f) return 0.0f;
+    unsigned b = fbits(a);
+    int ex = (int)((b >> 23) & 0xff) + k;
+    if (ex <= 0) return 0.0f;
+    if (ex >= 255) return bitsf((b & 0x80000000u) | 0x7f7fffffu);
+    return bitsf((b & 0x807fffffu) | ((unsigned)ex << 23));
+}
+MBX_HD double ldexp_ftz(double a, int k) {
+    if (a == 0.0) return 0.0;
+    uint64_t b = dbits(a);
+    int ex = (int)((b >> 52) & 0x7ff) + k;
+    if (ex <= 0) return 0.0;
+    if (ex >= 2047) return bitsd((b & 0x8000000000000000ull) | 0x7fefffffffffffffull);
+    return bitsd((b & 0x800fffffffffffffull) | ((uint64_t)ex << 52));
+}
+// Double-float forms: the exponent is the high part's.
+MBX_HD df32 ldexp_ftz(df32 a, int k) { return df32(ldexp_ftz(a.hi, k), ldexp_ftz(a.lo, k)); }
+MBX_HD TE<df32> te_norm(df32 m, int e) {
+    if (m.hi == 0.0f) return TE<df32>{df32(0.0f), 0};
+    const F32E h = te_norm(m.hi, e); // h.m = m.hi 2^(e - h.e)
+    return TE<df32>{df32(h.m, ldexp_ftz(m.lo, e - h.e)), h.e};
+}
+MBX_HD df32 fdiv_approx(df32 a, df32 b) { return a / b; }
+template <class T>
+MBX_HD T te_to_real(TE<T> a) { return ldexp_ftz(a.m, a.e); }
+template <class T>
+MBX_HD TE<T> te_mulr(TE<T> a, T b) { return te_norm(a.m * b, a.e); }
+template <class T>
+MBX_HD TE<T> te_from_fe(FE a) {
+    if (a.m == 0.0) return TE<T>{T(0), 0};
+    return te_norm((T)a.m, (int)a.e);
+}
+template <class T>
+MBX_HD FE fe_from_te(TE<T> a) { return a.m == T(0) ? fe_make(0.0, 0) : fe_make((double)a.m, (int64_t)a.e); }
+
+// Per-type constants of the lane.
+template <class T>
+struct LaneReal;
+template <>
+struct LaneReal<float> {
+    using V2 = float2;
+    static constexpr float kTinyX = 1e-30f;         // orbit entries below: exact floatexp step
+    static constexpr float kMinS = 7.888609e-31f;  // 2^-100: first step after a rebase needs s above this
+    static constexpr float kEscLo = 0.999998f;     // escape screen margins around R^2
+    static constexpr float kEscHi = 1.000002f;
+    static constexpr int kExpClamp = 120;
+    static constexpr bool kTrackError = true;
+    static constexpr float kEps2 = 7.105427e-15f; // 2 * (2^-24)^2: per-step rounding variance
+    using Z = float;                              // screens (|z|^2, |w|^2 and the like)
+    MBX_HD static V2 make2(float a, float b) { return make_float2(a, b); }
+    MBX_HD static float tof(float x) { return x; }
+    MBX_HD static float z(float x) { return x; }
+    MBX_HD static float zabs2(float a, float b) { return a * a + b * b; }
+};
+template <>
+struct LaneReal<double> {
+    using V2 = double2;
+    static constexpr double kTinyX = 1e-290;
+    static constexpr double kMinS = 9.332636185032189e-302; // 2^-1000
+    static constexpr double kEscLo = 1.0;
+    static constexpr double kEscHi = 1.0;
+    static constexpr int kExpClamp = 1000;
+    static constexpr bool kTrackError = false;
+    static constexpr float kEps2 = 0.0f;
+    using Z = double;
+    MBX_HD static V2 make2(double a, double b) { return make_double2(a, b); }
+    MBX_HD static float tof(double x) { return (float)x; }
+    MBX_HD static double z(double x) { return x; }
+    MBX_HD static double zabs2(double a, double b) { return a * a + b * b; }
+};
+template <>
+struct LaneReal<df32> {
+    using V2 = df2;
+    static constexpr float kTinyX = 1e-30f;         // as the FP32 lane: both parts must stay normal
+    static constexpr float kMinS = 8.673617e-19f;   // 2^-60
+    static constexpr float kEscLo = 0.999998f;     // screens run on the high parts, as in the FP32 lane
+    static constexpr float kEscHi = 1.000002f;
+    static constexpr int kExpClamp = 120;
+    static constexpr bool kTrackError = true;
+    static constexpr float kEps2 = 2.524355e-29f;   // 2 * (2^-48)^2
+    using Z = float;
+    MBX_HD static V2 make2(df32 a, df32 b) { return df2{a, b}; }
+    MBX_HD static float tof(df32 x) { return x.hi; }
+    MBX_HD static float z(df32 x) { return x.hi; }
+    MBX_HD static float zabs2(df32 a, df32 b) { return a.hi * a.hi + b.hi * b.hi; }
+};
+
+// Exact floatexp step for orbit entries below the lane type's range
+// (mp.cpp:2794-2835).
+MBX_HDF void exact_step(FE Xr, FE Xi, FE dcr, FE dci, FE& S, double& wr, double& wi) {
+    const double sm = S.m, sm2 = sm * sm;
+    const int64_t se = S.e;
+    const int64_t NONE = (int64_t)0x8000000000000000ll;
+    int64_t e = NONE;
+    const bool has_w = wr != 0.0 || wi != 0.0;
+    if (has_w && Xr.m != 0.0) e = lmax(e, Xr.e + se);
+    if (has_w && Xi.m != 0.0) e = lmax(e, Xi.e + se);
+    if (has_w) e = lmax(e, se + se);
+    if (dcr.m != 0.0) e = lmax(e, dcr.e);
+    if (dci.m != 0.0) e = lmax(e, dci.e);
+    if (e == NONE) {
+        S = fe_make(1.0, 0);
+        wr = wi = 0.0;
+        return;
+    }
+    auto align = [e](double m, int64_t te) -> double {
+        int64_t d = te - e;
+        if (m == 0.0 || d < -54) return 0.0;
+        return m * pow2i((int)d);
+    };
+    const double xs_r = align(Xr.m * sm, Xr.e + se);
+    const double xs_i = align(Xi.m * sm, Xi.e + se);
+    const double s2 = align(sm2, se + se);
+    const double cr = align(dcr.m, dcr.e);
+    const double ci = align(dci.m, dci.e);
+    const double nr = 2.0 * (xs_r * wr - xs_i * wi) + s2 * (wr * wr - wi * wi) + cr;
+    const double ni = 2.0 * (xs_r * wi + xs_i * wr) + 2.0 * s2 * wr * wi + ci;
+    const double mag = sqrt(nr * nr + ni * ni);
+    if (mag == 0.0) {
+        S = fe_make(1.0, 0);
+        wr = wi = 0.0;
+        return;
+    }
+    S = fe_renorm(mag, e);
+    wr = nr / mag;
+    wi = ni / mag;
+}
+
+// Floatexp copy of the FP64 BLA table: A and B as mantissa pairs with one
+// exponent each, the radius^2 as mantissa + exponent. Built once per reference
+// from the FP64 table (k_bla_to_lane).
+MBX_HD int dexp_of(double x) { // x = m 2^e, m in [0.5,1)
+    int e;
+    (void)xfrexp(x, &e);
+    return e;
+}
+
+template <class T>
+MBX_HDF BlaEntry<T> bla_entry(double v, double4 c) {
+    BlaEntry<T> b;
+    double amax = fmax(fabs(c.x), fabs(c.y)), bmax = fmax(fabs(c.z), fabs(c.w));
+    b.ea = amax > 0 ? dexp_of(amax) : 0;
+    b.eb = bmax > 0 ? dexp_of(bmax) : 0;
+    b.ar = (T)xldexp(c.x, -b.ea);
+    b.ai = (T)xldexp(c.y, -b.ea);
+    b.br = (T)xldexp(c.z, -b.eb);
+    b.bi = (T)xldexp(c.w, -b.eb);
+    if (v > 0.0) {
+        int e;
+        double m = xfrexp(v, &e);
+        b.r2m = (T)m;
+        b.r2e = e;
+        if (b.r2m >= T(1)) { // mantissa rounded up to 1.0
+            b.r2m = T(0.5);
+            b.r2e += 1;
+        }
+    } else {
+        b.r2m = T(0);
+        b.r2e = 0;
+    }
+    return b;
+}
+
+// BLA skip in floatexp (mp.cpp:2883-2970 semantics; coefficients and radii
+// constructed in FP64). dz = S w, dc = dcm 2^dce (shared exponent). amp2
+// receives |A|^2 (S_old / S_new)^2, the factor that carries a squared error of
+// w into the new units.
+template <class T>
+MBX_HDF int lane_bla(const BlaView& b, const BlaEntry<T>* t, const typename LaneReal<T>::V2* orb, bool periodic, int s, TE<T>& S, T& wr, T& wi,
+                     typename LaneReal<T>::V2 dcm, int dce, typename LaneReal<T>::Z ESC2lo, int mx_ref_it, float& amp2) {
+    using R = LaneReal<T>;
+    using Z = typename R::Z;
+    int maxp = b.nlev - 1;
+    int startp = (s == 1) ? maxp : ffs32(s - 1) - 1;
+    if (startp > maxp) startp = maxp;
+    if (startp < b.minlevel) return 0;
+    const Z wm2 = R::zabs2(wr, wi);
+    if (wm2 == Z(0)) return 0;
+    const TE<Z> dz2 = te_norm(R::z(S.m) * R::z(S.m) * wm2, 2 * S.e);
+    for (int p = startp; p >= b.minlevel; --p) {
+        int i = (s - 1) >> p;
+        if (i >= b.size[p]) continue;
+        const BlaEntry<T> e = t[b.off[p] + i];
+        if (e.r2m == T(0)) continue;
+        if (!(dz2.e < e.r2e || (dz2.e == e.r2e && dz2.m < R::z(e.r2m)))) continue; // |dz|^2 < r2
+        const int l = 1 << p;
+        const int land = s + l;
+        if (land >= mx_ref_it - 1) continue;
+        // A dz + B dc = A (S.m w) 2^(ea + S.e) + B dcm 2^(eb + dce)
+        const T swr = S.m * wr, swi = S.m * wi;
+        T t1r = e.ar * swr - e.ai * swi, t1i = e.ar * swi + e.ai * swr;
+        T t2r = e.br * dcm.x - e.bi * dcm.y, t2i = e.br * dcm.y + e.bi * dcm.x;
+        const int E1 = e.ea + S.e, E2 = e.eb + dce;
+        const int E = imax(E1, E2);
+        const T vr = ldexp_ftz(t1r, E1 - E) + ldexp_ftz(t2r, E2 - E);
+        const T vi = ldexp_ftz(t1i, E1 - E) + ldexp_ftz(t2i, E2 - E);
+        const T v2 = vr * vr + vi * vi;
+        // Never skip past an escape: z = X_land + dz' (conservative test).
+        const typename LaneReal<T>::V2 zl = orb[land];
+        const T zr = zl.x + ldexp_ftz(vr, E), zi = zl.y + ldexp_ftz(vi, E);
+        if (R::zabs2(zr, zi) > ESC2lo) return 0;
+        if (v2 == T(0)) {
+            if (!periodic) return 0;
+            S = TE<T>{T(0.5), 1};
+            wr = wi = T(0);
+            amp2 = 0.0f;
+        } else {
+            const T vm = tsqrt(v2), inv = T(1) / vm;
+            {
+                const float ar = R::tof(e.ar), ai = R::tof(e.ai), sm = R::tof(S.m);
+                amp2 = ldexp_ftz(fminf((ar * ar + ai * ai) * (sm * sm) / R::tof(v2), 1e38f), 2 * (E1 - E));
+            }
+            S = te_norm(vm, E);
+            wr = vr * inv;
+            wi = vi * inv;
+        }
+        return l;
+    }
+    return 0;
+}
+
+// Error model of the FP32 iteration: each FP32 step adds an independent
+// relative rounding error to the delta (variance 2 u^2, u = 2^-24: the RMS of
+// the step's roundings, measured against arbitrary-precision orbits), and an
+// existing error is carried by the map's derivative |2 z|. A rebase divides the
+// delta by |z| / |dz|, so it scales the relative error up by |dz| / |z|.
+// The estimate decides which results the FP32 pass may keep; the others leave
+// the pass for the FP64 rerun pass:
+//   * an escape whose iteration count the error could move: |z_N|^2 or
+//     |z_(N-1)|^2 within twice the estimated error of the bailout radius^2;
+//   * an interior decision (cycle found, or maxiter reached) with an estimated
+//     relative error above 1e-2;
+//   * any sample whose estimate exceeds 1/2 (its orbit is no longer known).
+// The double-float lane runs the same model with its own rounding variance and
+// sends what it cannot vouch for on to the FP64 lane. The estimate itself is
+// kept in float for every lane type.
+constexpr float kLaneInteriorTol2 = 1e-4f; // (1e-2)^2
+constexpr float kLaneCap2 = 0.25f;         // (1/2)^2
+
+// Squared relative error estimate of the delta.
+template <class T>
+MBX_HD float lane_rel_err2(float err2, T wr, T wi) {
+    const float a = LaneReal<T>::tof(wr), b = LaneReal<T>::tof(wi);
+    const float wm2 = a * a + b * b;
+    return wm2 > 0.0f ? err2 / wm2 : 0.0f;
+}
+template <class V2>
+MBX_HD float lane_abs2f(V2 v) {
+    const float a = (float)v.x, b = (float)v.y;
+    return a * a + b * b;
+}
+
+// Per-lane state of a lane pass.
+template <class T>
+struct Lane {
+    using V2 = typename LaneReal<T>::V2;
+    int i, oidx;         // pass entry, output index
+    double dpx, dpy;     // sample offset from the reference in pixels (for rare exact steps)
+    TE<T> S;             // delta scale
+    T wr, wi, s, dr, di;
+    V2 dcm;              // dc mantissas with shared exponent dce
+    int dce;
+    int m, iter, rm;
+    V2 Xc;               // X_m
+    // running rounding-error estimate: err2 = (error of w)^2 in units of S^2,
+    // g2 = |2 z|^2 at the current iterate (the step's error amplification)
+    float err2, g2;
+    // interior detection
+    float zsr_f, zsi_f, conf_D2;
+    T swr, swi;
+    double zsr, zsi, conf_zr, conf_zi;
+    TE<T> sS;
+    int save_iter, period_win, conf_P, conf_next, conf_count, conf_giveup, sidx, save_iter2, twin2;
+};
+
+template <class T>
+MBX_HD void lane_refresh(Lane<T>& L) {
+    L.s = te_to_real(L.S);
+    const T inv = fdiv_approx(T(1), L.S.m);
+    L.dr = ldexp_ftz(L.dcm.x * inv, L.dce - L.S.e);
+    L.di = ldexp_ftz(L.dcm.y * inv, L.dce - L.S.e);
+}
+
+// dz = S w with S <- |v| 2^e and w <- v / |v| for a vector v scaled by 2^e.
+template <class T>
+MBX_HD void lane_set_delta(Lane<T>& L, T vr, T vi, int e) {
+    const T v2 = vr * vr + vi * vi;
+    if (v2 == T(0)) {
+        L.S = TE<T>{T(0.5), 1};
+        L.wr = L.wi = T(0);
+        return;
+    }
+    const T vm = tsqrt(v2), inv = T(1) / vm;
+    L.S = te_norm(vm, e);
+    L.wr = vr * inv;
+    L.wi = vi * inv;
+}
+
+template <class T>
+MBX_HD FE lane_dc_re(const MixedParams& p, const Lane<T>& L) { return fe_mul_d(p.dxfe, L.dpx); }
+template <class T>
+MBX_HD FE lane_dc_im(const MixedParams& p, const Lane<T>& L) { return fe_mul_d(p.dyfe, L.dpy); }
+
+// Start sample arr = {row, col, subrow, subcol} as pass entry i.
+template <class T>
+MBX_HDF void lane_setup_at(Lane<T>& L, int i, const int* arr, const MixedParams& p, const TE<T> dxf, const TE<T> dyf, const typename LaneReal<T>::V2* orb) {
+    const FrameGeom& g = p.g;
+    L.i = i;
+    L.oidx = (arr[0] * g.sub + g.sub / 2 + arr[2]) * g.W * g.sub + (arr[1] * g.sub + g.sub / 2 + arr[3]);
+    L.dpx = arr[1] + (double)arr[3] / g.sub - p.ref_x;
+    L.dpy = arr[0] + (double)arr[2] / g.sub - p.ref_y;
+    // dc in floatexp with one shared exponent.
+    const TE<T> cr = te_mulr(dxf, (T)L.dpx), ci = te_mulr(dyf, (T)L.dpy);
+    int e = (cr.m != T(0)) ? cr.e : ((ci.m != T(0)) ? ci.e : 0);
+    if (cr.m != T(0) && ci.m != T(0)) e = imax(cr.e, ci.e);
+    L.dce = e;
+    L.dcm = LaneReal<T>::make2(ldexp_ftz(cr.m, cr.e - e), ldexp_ftz(ci.m, ci.e - e));
+    lane_set_delta(L, L.dcm.x, L.dcm.y, e);
+    lane_refresh(L);
+    L.m = 1;
+    L.iter = 1;
+    L.rm = 0;
+    L.Xc = orb[0];
+    L.zsr = L.zsi = 1e30;
+    L.zsr_f = L.zsi_f = 1e30f;
+    L.conf_zr = L.conf_zi = 0.0;
+    L.conf_D2 = 0.0f;
+    L.save_iter = 1;
+    L.period_win = 1;
+    L.conf_P = L.conf_next = L.conf_count = L.conf_giveup = 0;
+    L.swr = L.swi = T(3e38);
+    L.sS = TE<T>{T(2), 0};
+    L.sidx = -2;
+    L.save_iter2 = 1;
+    L.twin2 = 1;
+    L.err2 = LaneReal<T>::kEps2;
+    L.g2 = 4.0f * lane_abs2f(L.Xc);
+}
+
+template <class T>
+MBX_HDF void lane_setup(Lane<T>& L, int i, const DeviceFrame& f, const MixedParams& p, const TE<T> dxf, const TE<T> dyf, const typename LaneReal<T>::V2* orb) {
+    int arr[4];
+    entry_coords(f.px, i, arr);
+    lane_setup_at(L, i, arr, p, dxf, dyf, orb);
+}
+
+// (a / b)^2 as float, saturating: converts err2 from units of a^2 to b^2.
+template <class T>
+MBX_HD float lane_scale_ratio2(TE<T> a, TE<T> b) {
+    const float bm = LaneReal<T>::tof(b.m);
+    if (bm == 0.0f) return 0.0f;
+    const float r = LaneReal<T>::tof(a.m) / bm;
+    return ldexp_ftz(r * r, imax(-300, imin(300, 2 * (a.e - b.e))));
+}
+
+// z = X_m + S w in FP64 (rare decisions).
+template <class T>
+MBX_HD void lane_z_double(const Lane<T>& L, const double2* Zd, double& zr, double& zi) {
+    const double2 Xd = L.m ? Zd[L.rm] : make_double2(0.0, 0.0);
+    const double sd = xldexp((double)L.S.m, L.S.e);
+    zr = Xd.x + sd * (double)L.wr;
+    zi = Xd.y + sd * (double)L.wi;
+}
+
+// Interior decision: an FP32 lane whose error estimate is too large leaves
+// for the FP64 pass (3) instead of reporting interior (2).
+template <class T>
+MBX_HD int lane_interior(const Lane<T>& L) {
+    if (LaneReal<T>::kTrackError && lane_rel_err2(L.err2, L.wr, L.wi) > kLaneInteriorTol2) return 3;
+    return 2;
+}
+
+// Advance one lane by up to `budget` iterations. Returns 0 running, 1 escaped,
+// 2 interior, 3 precision spent (FP32 lane only: rerun in FP64); zrad_out is
+// set on escape.
+template <class T>
+MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
+                     int reflen, T ESC2f, int blamask, T& zrad_out, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip,
+                     unsigned long long& n_rebase) {
+    using R = LaneReal<T>;
+    using Z = typename R::Z;
+    const FrameGeom& g = p.g;
+    const int per = p.per;
+    const double2* Zd = f.orbit.Z;
+    const FE2* Zfe = f.orbit.Zfe;
+    (void)ESC2f;
+    const Z ESC2z = (Z)g.ESC2;
+    const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
+    for (int b = 0; b < budget; ++b) {
+        if (L.iter >= g.mxit) return lane_interior(L);
+        if (p.use_interior) {
+            const int idxs = per ? L.rm : L.m;
+            if (idxs == L.sidx && L.wr == L.swr && L.wi == L.swi && L.S.m == L.sS.m && L.S.e == L.sS.e) return lane_interior(L);
+            if (L.iter - L.save_iter2 >= L.twin2) {
+                L.swr = L.wr;
+                L.swi = L.wi;
+                L.sS = L.S;
+                L.sidx = idxs;
+                L.save_iter2 = L.iter;
+                L.twin2 += L.twin2;
+            }
+        }
+        if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
+            float amp2 = 0.0f;
+            const int skip = lane_bla(f.bla, blat, orb, per > 0, L.rm, L.S, L.wr, L.wi, L.dcm, L.dce, ESC2lo, per ? per : reflen, amp2);
+            if (skip > 0) {
+                ++n_bla;
+                n_skip += skip;
+                L.m += skip;
+                L.iter += skip;
+                L.rm += skip;
+                if (per && L.rm >= per) L.rm -= per;
+                lane_refresh(L);
+                L.Xc = orb[L.rm];
+                if (R::kTrackError) {
+                    // the skip carries the error by A; |w| is 1 afterwards
+                    L.err2 = L.err2 * amp2 + R::kEps2;
+                    L.g2 = 4.0f * lane_abs2f(L.Xc);
+                }
+                L.zsr = L.zsi = 1e30;
+                L.zsr_f = L.zsi_f = 1e30f;
+                L.save_iter = L.iter;
+                L.period_win = 1;
+                L.conf_P = 0;
+                L.conf_giveup = 0;
+                continue;
+            }
+        }
+        ++n_steps;
+        // w' = (2 X_m + s w) w + d. Exact floatexp step where the lane type
+        // would lose a term: the orbit entry below its range, or the first
+        // step after a rebase (X = 0, |w| = 1) when s = |dz| is too small a
+        // normal number, where dz^2 can be as large as dc (z ~ sqrt(minibrot
+        // size) at a nucleus pass).
+        const bool tiny = (L.m == 0 && !(L.s >= R::kMinS)) ||
+                          (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0));
+        if (!tiny) {
+            const T fR = T(2) * L.Xc.x + L.s * L.wr;
+            const T fI = T(2) * L.Xc.y + L.s * L.wi;
+            const T nwr = fR * L.wr - fI * L.wi + L.dr;
+            const T nwi = fR * L.wi + fI * L.wr + L.di;
+            L.wr = nwr;
+            L.wi = nwi;
+            if (R::kTrackError) {
+                const float a = R::tof(nwr), c = R::tof(nwi);
+                L.err2 = L.err2 * L.g2 + R::kEps2 * (a * a + c * c);
+            }
+        } else {
+            double wr = (double)L.wr, wi = (double)L.wi;
+            const FE S0 = fe_from_te(L.S);
+            FE S = S0;
+            const FE zero = fe_make(0.0, 0);
+            const FE Xr = L.m ? Zfe[L.rm].re : zero, Xi = L.m ? Zfe[L.rm].im : zero;
+            exact_step(Xr, Xi, lane_dc_re(p, L), lane_dc_im(p, L), S, wr, wi);
+            if (R::kTrackError) {
+                // error carried into the new units: |2 z|^2 (S0 / S)^2 err2,
+                // z = X + S0 w in floatexp (z may lie below FP32's range)
+                const FE zr = fe_add(Xr, fe_mul_d(S0, (double)L.wr)), zi = fe_add(Xi, fe_mul_d(S0, (double)L.wi));
+                const FE z2 = fe_add(fe_mul(zr, zr), fe_mul(zi, zi));
+                const FE q = fe_div(S0, S);
+                const double amp = S.m == 0.0 ? 0.0 : 4.0 * fe_to_double(fe_mul(z2, fe_mul(q, q)));
+                L.err2 = (float)fmin(amp * (double)L.err2, 3e38) + R::kEps2;
+            }
+            L.S = te_from_fe<T>(S);
+            L.wr = (T)wr;
+            L.wi = (T)wi;
+            lane_refresh(L);
+        }
+        ++L.m;
+        ++L.iter;
+        ++L.rm;
+        if (per && L.rm == per) L.rm = 0;
+        L.Xc = orb[L.rm];
+        const T zr = L.Xc.x + L.s * L.wr, zi = L.Xc.y + L.s * L.wi;
+        const Z zrad = R::zabs2(zr, zi);
+        if (zrad > ESC2lo) {
+            Z zesc = zrad;
+            bool esc = zrad > ESC2hi;
+            if (!esc) {
+                double zdr, zdi;
+                lane_z_double(L, Zd, zdr, zdi);
+                const double zr2 = zdr * zdr + zdi * zdi;
+                esc = zr2 > g.ESC2;
+                zesc = (Z)zr2;
+            }
+            if (esc) {
+                zrad_out = T(zesc);
+                if (R::kTrackError) {
+                    // Keep N only if the estimated error of |z|^2 (2 rho |dz| / |z|,
+                    // doubled) cannot carry |z_N|^2 or |z_(N-1)|^2 across the bailout.
+                    const float sf = R::tof(L.s), wrf = R::tof(L.wr), wif = R::tof(L.wi), zf = (float)zesc, Ef = (float)ESC2z;
+                    const float dzm2 = sf * sf * (wrf * wrf + wif * wif);
+                    const float amb = 4.0f * sqrtf(lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
+                    if (zf < Ef * (1.0f + amb) || 0.25f * L.g2 > Ef * (1.0f - amb)) return 3;
+                }
+                return 1;
+            }
+        }
+        if (p.use_interior) {
+            if (L.conf_P > 0) {
+                L.conf_D2 *= 4.0f * (float)zrad;
+                if (L.conf_D2 > 1e18f) L.conf_D2 = 1e18f;
+                if (L.iter >= L.conf_next) {
+                    double zdr, zdi;
+                    lane_z_double(L, Zd, zdr, zdi);
+                    const double qr = zdr - L.conf_zr, qi = zdi - L.conf_zi;
+                    if (qr * qr + qi * qi < p.interior_eps2 * (zdr * zdr + zdi * zdi) && L.conf_D2 < 1.0f) {
+                        if (++L.conf_count >= p.interior_confirm) return lane_interior(L);
+                        L.conf_zr = zdr;
+                        L.conf_zi = zdi;
+                        L.conf_D2 = 1.0f;
+                        L.conf_next = L.iter + L.conf_P;
+                    } else {
+                        L.conf_P = 0;
+                        ++L.conf_giveup;
+                    }
+                }
+            } else if ((L.iter & 15) == 0 && L.conf_giveup < 3) {
+                const float zrf = R::tof(zr), zif = R::tof(zi);
+                const float qr = zrf - L.zsr_f, qi = zif - L.zsi_f;
+                const bool maybe = qr * qr + qi * qi < 1e-11f * (float)zrad;
+                const bool save = L.iter - L.save_iter >= L.period_win;
+                if (maybe || save) {
+                    double zdr, zdi;
+                    lane_z_double(L, Zd, zdr, zdi);
+                    if (maybe) {
+                        const double dqr = zdr - L.zsr, dqi = zdi - L.zsi;
+                        if (dqr * dqr + dqi * dqi < p.interior_eps2 * (zdr * zdr + zdi * zdi)) {
+                            L.conf_P = imax(L.iter - L.save_iter, 1);
+                            L.conf_zr = zdr;
+                            L.conf_zi = zdi;
+                            L.conf_D2 = 1.0f;
+                            L.conf_next = L.iter + L.conf_P;
+                            L.conf_count = 0;
+                        }
+                    }
+                    if (save) {
+                        L.zsr = zdr;
+                        L.zsi = zdi;
+                        L.zsr_f = zrf;
+                        L.zsi_f = zif;
+                        L.save_iter = L.iter;
+                        L.period_win += L.period_win;
+                    }
+                }
+            }
+        }
+        if (R::kTrackError) L.g2 = 4.0f * (float)zrad;
+        // keep |w| ~ 1 (rescale window [1/wmax2, wmax2], autotuned); the scale
+        // factor only needs to be near |w|, as long as S and w change by it
+        // and its exact reciprocal
+        const Z wm2 = R::zabs2(L.wr, L.wi);
+        if (R::kTrackError && wm2 > Z(0) && L.err2 > kLaneCap2 * (float)wm2) return 3; // precision spent
+        if (wm2 > Z(p.wmax2) || (wm2 < Z(p.wmin2) && wm2 > Z(0))) {
+            const T wmag = T(tsqrt(wm2)), inv = T(1) / wmag;
+            L.S = te_mulr(L.S, wmag);
+            L.wr *= inv;
+            L.wi *= inv;
+            if (R::kTrackError) L.err2 *= R::tof(inv) * R::tof(inv);
+            lane_refresh(L);
+        }
+        // Rebase (mp.cpp:3584-3615): |z|^2 < |dz|^2 decided on floatexp with a
+        // 1e-4 margin; FP64 floatexp inside the margin, for strong
+        // cancellation in X + dz, and at the end of the reference.
+        const Z w2 = R::zabs2(L.wr, L.wi);
+        int decide = 0; // 0 none, 1 rebase in the lane type, 2 FP64 floatexp test
+        // Screen: |dz|^2 < |X|^2 / 5 means |z| > |dz| (no rebase). s = 0 when S
+        // is below the type's range, where |dz|^2 <= 2^-252 wmax2 is far below
+        // any |X|^2 above kTinyX^2.
+        const Z xr2 = R::zabs2(L.Xc.x, L.Xc.y);
+        const Z sz = R::z(L.s);
+        const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * w2 < Z(0.2) * xr2;
+        const TE<Z> dz2 = far ? TE<Z>{Z(0), 0} : te_norm(R::z(L.S.m) * R::z(L.S.m) * w2, 2 * L.S.e);
+        if (!per && L.m >= reflen) decide = 2;
+        else if (!far && dz2.m != Z(0)) {
+            if (zrad == Z(0)) decide = 2;
+            else {
+                // q = |z|^2 / |dz|^2 compared with 1 -/+ 1e-4 without a division:
+                // z2.m 2^(z2.e - dz2.e) against dz2.m (1 -/+ 1e-4)
+                const TE<Z> z2 = te_norm(zrad, 0);
+                const Z zq = ldexp_ftz(z2.m, imax(-R::kExpClamp, imin(R::kExpClamp, z2.e - dz2.e)));
+                if (zq < Z(0.9999) * dz2.m) decide = (zrad > Z(0.25) * xr2 && L.s != T(0)) ? 1 : 2;
+                else if (zq < Z(1.0001) * dz2.m) decide = 2;
+            }
+        }
+        const TE<T> S0 = L.S;
+        if (decide == 1) {
+            lane_set_delta(L, zr, zi, 0);
+            lane_refresh(L);
+            if (R::kTrackError) L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2;
+            L.m = 0;
+            L.rm = -1;
+            L.Xc = R::make2(T(0), T(0));
+            ++n_rebase;
+        } else if (decide == 2) {
+            const FE S = fe_from_te(L.S);
+            FE Xmr = L.m ? Zfe[L.rm].re : fe_make(0.0, 0);
+            FE Xmi = L.m ? Zfe[L.rm].im : fe_make(0.0, 0);
+            FE Swr = fe_mul_d(S, (double)L.wr), Swi = fe_mul_d(S, (double)L.wi);
+            FE zrfe = fe_add(Xmr, Swr), zife = fe_add(Xmi, Swi);
+            FE zradfe = fe_add(fe_mul(zrfe, zrfe), fe_mul(zife, zife));
+            FE dzfe = fe_add(fe_mul(Swr, Swr), fe_mul(Swi, Swi));
+            if ((!per && L.m >= reflen) || fe_abs_less(zradfe, dzfe)) {
+                FE Snew = fe_sqrt(zradfe);
+                if (Snew.m == 0.0) {
+                    L.wr = L.wi = T(0);
+                } else {
+                    L.S = te_from_fe<T>(Snew);
+                    L.wr = (T)fe_to_double(fe_div(zrfe, Snew));
+                    L.wi = (T)fe_to_double(fe_div(zife, Snew));
+                    lane_refresh(L);
+                    if (R::kTrackError) L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2;
+                }
+                L.m = 0;
+                L.rm = -1;
+                L.Xc = R::make2(T(0), T(0));
+                ++n_rebase;
+            }
+        }
+    }
+    return 0;
+}
+
+} // namespace mbx

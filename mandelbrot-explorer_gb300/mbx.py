@@ -101,6 +101,10 @@ class Stats(ctypes.Structure):
         ("pass_gpu_ms", ctypes.c_double),
         ("reused_reference", ctypes.c_int),
         ("rebases", ctypes.c_longlong),
+        ("fp64_reruns", ctypes.c_longlong),
+        ("rerun_gpu_ms", ctypes.c_double),
+        ("fp64_reruns_fp64", ctypes.c_longlong),
+        ("rerun_fp64_gpu_ms", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -123,6 +127,7 @@ EXPORTS = (
     "mbx_render_shallow_noalloc",
     "mbx_set_tuning",
     "mbx_autotune",
+    "mbx_compute_batch",
 )
 
 _lib = None
@@ -161,6 +166,8 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
         lib.mbx_autotune.restype = ctypes.c_int
         lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
+        lib.mbx_compute_batch.restype = ctypes.c_int
+        lib.mbx_compute_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.c_int, ctypes.POINTER(Stats), ctypes.POINTER(Stats)]
         lib.mbx_render_shallow_noalloc.restype = ctypes.c_int
         lib.mbx_render_shallow_noalloc.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 4
         lib.mbx_find_nucleus.restype = ctypes.c_int
@@ -347,6 +354,19 @@ class CudaComputeBackend:
     def compute(self, req: ComputeRequest) -> bool:
         """True on success, like IComputeBackend::compute."""
         return self.compute_status(req) == OK
+
+    def compute_batch(self, reqs) -> int:
+        """Renders several frames with shared passes (mbx_compute_batch).
+        Sets last_view_stats (one Stats per frame) and last_batch_stats."""
+        built = [self._build(q) for q in reqs]
+        arr = (_Request * len(built))(*[b[0] for b in built])
+        vst = (Stats * len(built))()
+        bst = Stats()
+        rc = self._lib.mbx_compute_batch(self._ctx, arr, len(built), vst, ctypes.byref(bst))
+        self.last_view_stats = list(vst)
+        self.last_batch_stats = bst
+        self.last_status = rc
+        return rc
 
 
 def create_compute_backend(requested: str = "cuda", device: int = 0) -> CudaComputeBackend:

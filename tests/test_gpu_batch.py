@@ -1,0 +1,72 @@
+"""Batched rendering (mbx_compute_batch): several frames of different sizes and
+depths share one probe and one main launch sequence (a CUDA graph). Every
+frame must come out identical to rendering it alone with mbx_compute, and a
+replay of the same batch identical to the first run."""
+import numpy as np
+import pytest
+
+import mbx
+import views
+from conftest import load_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _req(v, w, h, mode=mbx.PRECISION_MIXED):
+    return mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], w, h, v["max_iterations"], bailout=v["bailout"], precision_mode=mode)
+
+
+def _frames():
+    c = load_cases()
+    mb = c["minibrot875"]
+    sp = c["subpixel737"]
+    return [
+        (views.deep_view(300), 240, 135),
+        (views.deep_view(1000), 160, 90),
+        (dict(center_re=mb["center_re"], center_im=mb["center_im"], scale=mb["scale"], max_iterations=mb["max_iterations"], bailout=mb["bailout"]), 24, 18),
+        (dict(center_re=sp["center_re"], center_im=sp["center_im"], scale=sp["scale"], max_iterations=sp["max_iterations"], bailout=sp["bailout"]), 48, 36),
+        (views.c1_view(), 64, 36),  # not a floatexp frame: rendered on its own inside the batch
+    ]
+
+
+def test_batch_matches_single_frames():
+    be = mbx.create_compute_backend("cuda")
+    frames = _frames()
+    singles = []
+    for v, w, h in frames:
+        r = _req(v, w, h)
+        assert be.compute_status(r) == mbx.OK, be.last_error()
+        singles.append((r.iterations.copy(), r.escape_iteration.copy()))
+    for rep in range(2):  # the second run replays the captured graph
+        reqs = [_req(v, w, h) for v, w, h in frames]
+        rc = be.compute_batch(reqs)
+        assert rc == mbx.OK, be.last_error()
+        bs = be.last_batch_stats.as_dict()
+        assert bs["kernel_launches"] == 7 and bs["passes"] == 2
+        for (it, en), r, (v, w, h) in zip(singles, reqs, frames):
+            assert np.array_equal(r.escape_iteration, en), (rep, w, h)
+            assert np.array_equal(r.iterations, it), (rep, w, h)
+        print("\n[batch] run %d: samples %d, fp32 reruns %d, fp64 reruns %d, shared passes %.3f ms" % (rep, bs["samples"], bs["fp64_reruns"], bs["fp64_reruns_fp64"], bs["pass_gpu_ms"]))
+    be.close()
+
+
+def test_batch_device_outputs_and_invalid():
+    torch = pytest.importorskip("torch")
+    be = mbx.create_compute_backend("cuda")
+    frames = _frames()[:2]
+    reqs, host = [], []
+    for v, w, h in frames:
+        n = w * h
+        reqs.append(mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], w, h, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED,
+                                       iterations=torch.empty(n, dtype=torch.float32, device="cuda"), escape_iteration=torch.empty(n, dtype=torch.int32, device="cuda")))
+        r = _req(v, w, h)
+        assert be.compute_status(r) == mbx.OK
+        host.append(r.escape_iteration.copy())
+    assert be.compute_batch(reqs) == mbx.OK, be.last_error()
+    for r, en in zip(reqs, host):
+        assert np.array_equal(r.escape_iteration.cpu().numpy(), en)
+    bad = _req(*frames[0])
+    bad.sub = 2
+    assert be.compute_batch([_req(*frames[1]), bad]) == mbx.E_INVALID
+    assert "request 1" in be.last_error()
+    be.close()

@@ -51,39 +51,70 @@ def test_mixed_vs_truth(backend, k):
     ext = (tn > 0) & (men[idx] > 0)
     maxdmu = float(np.max(np.abs(mit[idx][ext].astype(np.float64) - tv[ext]), initial=0.0))
     full_same = np.mean(men == een)
-    print("\n[accuracy] 1e-%d: mixed N==truth %.5f  exact N==truth %.5f  class mismatches %d  max |dmu| %.3g  mixed==exact (full frame) %.5f  subset %d" % (k, m_same, e_same, cls, maxdmu, full_same, SUBSET))
+    print("\n[accuracy] 1e-%d: mixed N==truth %.5f  exact N==truth %.5f  class mismatches %d  max |dmu| %.3g  mixed==exact (full frame) %.5f  subset %d  fp64 reruns %d" % (k, m_same, e_same, cls, maxdmu, full_same, SUBSET, mst["fp64_reruns"]))
     assert cls == 0
     assert m_same >= 0.999
 
 
+# Tolerances the reference's verify harness applies to its own engine against
+# each arbitrary-precision golden (verify.cpp:11837-11881, gui case :376):
+# class-exact, and (max, mean, p99) of |smooth value difference|.
+TRUTH_TOL = {
+    "minibrot875": (1.0, None, None),
+    "extref875": (1.0, None, None),
+    "gui875": (1.0, None, None),
+    "slowpoint": (90000.0, 300.0, 3000.0),
+    "point31": (12000.0, 200.0, 4000.0),
+}
+
+
 def test_mixed_on_parity_cases(backend):
-    """Floatexp parity cases in mixed precision: against the reference's own
-    arbitrary-precision golden files with the tolerances its verify harness
-    applies to its engine (verify.cpp:11837-11857), and class-exact against the
-    exact form elsewhere."""
+    """Every perturbation parity case in mixed precision. Cases with the
+    reference's arbitrary-precision golden files are held to the tolerances its
+    verify harness applies to its engine (TRUTH_TOL); the others to class
+    agreement with the exact form and 99.9 % identical escape iterations. DE
+    colourings have no FP32 form and must come out identical to the exact form;
+    frames shallower than the floatexp range take the exact form too."""
     from conftest import GOLDEN
 
     cases = load_cases()
-    for name in ("minibrot875", "extref875", "deep876", "exterior1000", "subpixel737"):
-        c = cases[name]
+    for name, c in cases.items():
+        if len(c["scale"].split(".")[0]) <= 7:  # scale <= 1e6: the shallow path, not perturbation
+            continue
         r = {}
         for mode in (mbx.PRECISION_MIXED, mbx.PRECISION_EXACT):
-            req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], bailout=c["bailout"], precision_mode=mode)
+            req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"],
+                                     sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"], precision_mode=mode)
             assert backend.compute_status(req) == mbx.OK, backend.last_error()
-            r[mode] = (req.iterations, req.escape_iteration)
-        mi, mn = r[mbx.PRECISION_MIXED]
-        ei, en = r[mbx.PRECISION_EXACT]
-        same = np.mean(mn == en)
-        cls = int(np.sum((mn < 0) != (en < 0)))
-        msg = "[mixed vs exact] %s: N identical %.4f, class mismatches %d" % (name, same, cls)
+            r[mode] = (req.iterations, req.escape_iteration, backend.last_stats.as_dict())
+        mi, mn, mst = r[mbx.PRECISION_MIXED]
+        ei, en, _ = r[mbx.PRECISION_EXACT]
+        if c["coloring_method"] & (2 | 64):
+            assert np.array_equal(mi, ei) and np.array_equal(mn, en), name
+            print("\n[mixed vs exact] %s: DE colouring, exact form used" % name)
+            continue
+        both = (mi > -5) & (ei > -5)
+        same = np.mean(mn[both] == en[both])
+        cls = int(np.sum((mi[both] < -1.5) != (ei[both] < -1.5)))
+        msg = "[mixed vs exact] %s: N identical %.4f, class mismatches %d, fp64 reruns %d of %d" % (name, same, cls, mst["fp64_reruns"], mi.size)
         truth_path = os.path.join(GOLDEN, "truth_%s.f32" % name)
         if os.path.exists(truth_path):
             t = np.fromfile(truth_path, dtype="<f4")
-            ext = (t > -1.5) & (mi > -1.5)
-            tcls = int(np.sum((mi < -1.5) != (t < -1.5)))
-            d = float(np.max(np.abs(mi[ext].astype(np.float64) - t[ext]), initial=0.0))
-            msg += "; vs truth: class mismatches %d, max |dmu| %.4f" % (tcls, d)
+            valid = (t > -5) & (mi > -5)
+            ext = valid & (t > -1.5) & (mi > -1.5)
+            tcls = int(np.sum((mi[valid] < -1.5) != (t[valid] < -1.5)))
+            dd = np.abs(mi[ext].astype(np.float64) - t[ext])
+            d = float(np.max(dd, initial=0.0))
+            mean = float(dd.mean()) if dd.size else 0.0
+            p99 = float(np.sort(dd)[int(np.ceil(0.99 * dd.size)) - 1]) if dd.size else 0.0
+            msg += "; vs truth: class mismatches %d, |dmu| max %.4f mean %.4f p99 %.4f" % (tcls, d, mean, p99)
+            print("\n" + msg)
+            tmax, tmean, tp99 = TRUTH_TOL[name]
             assert tcls == 0, name
-            assert d <= 1.0, name
-        print("\n" + msg)
-        assert cls == 0, name
+            assert d <= tmax, name
+            assert tmean is None or mean <= tmean, name
+            assert tp99 is None or p99 <= tp99, name
+        else:
+            print("\n" + msg)
+            assert cls <= max(1, mi.size // 1000), name
+            assert same >= 0.999, name
