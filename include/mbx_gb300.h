@@ -143,6 +143,22 @@ int mbx_find_nucleus(const char* center_re, const char* center_im, const char* r
  * passes' counters go to batch_stats. Frames need fewer than 65536 sample rows. */
 int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats);
 
+/* Learned ordering of the batched main pass (no reference counterpart). With
+ * mode 1, each batch's main-pass samples start in decreasing cost as predicted
+ * by a BF16 MLP (24 -> 64 -> 64 -> 1) from the probe pass's costs around them;
+ * after the pass the model trains on the batch's measured per-sample costs
+ * (tensor-core kernels, Adam), so the next batch uses it. Mode 2 orders with
+ * the model as it stands (no training). An untrained model keeps the natural
+ * order. Outputs are identical in every mode. 0 (default): natural order. */
+int mbx_set_batch_scheduling(mbx_context* ctx, int mode);
+
+/* Diagnostics of the ordering model: parameters (5825 floats: W1 [64][24], b1
+ * [64], W2 [64][64], b2 [64], w3 [64], b3) set and/or read, and the gradients
+ * of one training step (mean squared error / 2 over the first 128 of n >= 128
+ * samples: features n x 24, targets n) without an update. */
+int mbx_schedule_params(mbx_context* ctx, const float* set, float* get);
+int mbx_schedule_gradient(mbx_context* ctx, const float* features, const float* targets, int n, float* grad);
+
 /* Allocation-free render of a shallow frame (no reference counterpart: the
  * reference has no device and allocates its buffers itself). For callers that
  * cannot allocate device memory: the caller passes the frame geometry — the

@@ -35,9 +35,11 @@ def units():
         ("kernels_exact.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "kernels_exact.cu")]),
         ("kernels_mixed.o", [NVCC] + common_nv + ["-fmad=true", "-c", os.path.join(SRC, "kernels_mixed.cu")]),
         ("noalloc.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "noalloc.cu")]),
+        ("order_model.o", [NVCC] + common_nv + ["-fmad=true", "-c", os.path.join(SRC, "order_model.cu")]),
         ("engine.o", cxx + ["-c", os.path.join(SRC, "engine.cpp")]),
         ("capi.o", cxx + ["-c", os.path.join(SRC, "capi.cpp")]),
         ("batch.o", cxx + ["-c", os.path.join(SRC, "batch.cpp")]),
+        ("parmul.o", cxx + ["-c", os.path.join(SRC, "parmul.cpp")]),
     ]
 
 

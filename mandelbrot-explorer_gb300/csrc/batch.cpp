@@ -22,7 +22,9 @@ BatchRunner::~BatchRunner() {
     if (st_) cudaStreamSynchronize(st_);
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
-    for (void* p : {(void*)d_probe_, (void*)d_main_, (void*)d_ctr_, (void*)d_view_interior_, (void*)d_qa_, (void*)d_qb_})
+    for (void* p : {(void*)d_probe_, (void*)d_main_, (void*)d_ctr_, (void*)d_view_interior_, (void*)d_qa_, (void*)d_qb_, (void*)d_qo_, (void*)d_main_total_,
+                    (void*)sched_.params, (void*)sched_.adam_m, (void*)sched_.adam_v, (void*)sched_.ready, (void*)sched_.steps, (void*)sched_.loss,
+                    (void*)sched_.hist, (void*)sched_.cursor, (void*)sched_.bucket, (void*)sched_.X, (void*)sched_.T})
         if (p) cudaFree(p);
     if (h_desc_) cudaFreeHost(h_desc_);
     if (h_ctr_) cudaFreeHost(h_ctr_);
@@ -84,10 +86,17 @@ int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err)
         }
     }
     if (capacity > cap_samples_) {
-        if (d_qa_) cudaFree(d_qa_);
-        if (d_qb_) cudaFree(d_qb_);
-        d_qa_ = d_qb_ = nullptr;
-        if (cudaMalloc(&d_qa_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&d_qb_, sizeof(uint64_t) * capacity) != cudaSuccess) {
+        for (uint64_t** q : {&d_qa_, &d_qb_, &d_qo_}) {
+            if (*q) cudaFree(*q);
+            *q = nullptr;
+        }
+        if (sched_.bucket) cudaFree(sched_.bucket);
+        if (sched_.hist) cudaFree(sched_.hist);
+        sched_.bucket = nullptr;
+        sched_.hist = nullptr;
+        if (cudaMalloc(&d_qa_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&d_qb_, sizeof(uint64_t) * capacity) != cudaSuccess ||
+            cudaMalloc(&d_qo_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&sched_.bucket, capacity + 8 * 1024) != cudaSuccess ||
+            cudaMalloc(&sched_.hist, sizeof(unsigned) * 32 * ((capacity + 8 * 1024 - 1) / 1024 + 8)) != cudaSuccess) {
             err = "batch queue allocation failed";
             cap_samples_ = 0;
             return MBX_E_NOMEM;
@@ -95,11 +104,103 @@ int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err)
         cap_samples_ = capacity;
         g_views_ = -1;
     }
+    if (!d_main_total_ && cudaMalloc(&d_main_total_, sizeof(unsigned)) != cudaSuccess) {
+        err = "batch counter allocation failed";
+        return MBX_E_NOMEM;
+    }
     return MBX_OK;
 }
 
+int BatchRunner::ensure_sched(std::string& err) {
+    if (sched_ready_) return MBX_OK;
+    if (!st_) {
+        int rc = ensure_engines(1, err);
+        if (rc != MBX_OK) return rc;
+    }
+    const int N = SchedLayout::N;
+    if (cudaMalloc(&sched_.params, sizeof(float) * N) != cudaSuccess || cudaMalloc(&sched_.adam_m, sizeof(float) * N) != cudaSuccess ||
+        cudaMalloc(&sched_.adam_v, sizeof(float) * N) != cudaSuccess || cudaMalloc(&sched_.ready, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&sched_.steps, sizeof(int)) != cudaSuccess || cudaMalloc(&sched_.loss, sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&sched_.cursor, sizeof(unsigned) * 32) != cudaSuccess ||
+        cudaMalloc(&sched_.X, sizeof(__nv_bfloat16) * kSchedSamples * kSchedFeatures) != cudaSuccess ||
+        cudaMalloc(&sched_.T, sizeof(float) * kSchedSamples) != cudaSuccess) {
+        err = "scheduler allocation failed";
+        return MBX_E_NOMEM;
+    }
+    cudaError_t e = sched_init(sched_, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return cuda_fail(err, "scheduler initialisation", e);
+    sched_ready_ = true;
+    return MBX_OK;
+}
+
+int BatchRunner::set_schedule(int mode, std::string& err) {
+    if (mode < 0 || mode > 2) {
+        err = "scheduling mode must be 0, 1 or 2";
+        return MBX_E_INVALID;
+    }
+    if (mode != 0) {
+        int rc = ensure_sched(err);
+        if (rc != MBX_OK) return rc;
+    }
+    schedule_ = mode;
+    return MBX_OK;
+}
+
+int BatchRunner::schedule_params(const float* set, float* get, std::string& err) {
+    int rc = ensure_sched(err);
+    if (rc != MBX_OK) return rc;
+    const size_t bytes = sizeof(float) * SchedLayout::N;
+    if (set) {
+        cudaMemcpyAsync(sched_.params, set, bytes, cudaMemcpyHostToDevice, st_);
+        cudaMemsetAsync(sched_.adam_m, 0, bytes, st_);
+        cudaMemsetAsync(sched_.adam_v, 0, bytes, st_);
+    }
+    if (get) cudaMemcpyAsync(get, sched_.params, bytes, cudaMemcpyDeviceToHost, st_);
+    cudaError_t e = cudaStreamSynchronize(st_);
+    return e == cudaSuccess ? MBX_OK : cuda_fail(err, "scheduler parameters", e);
+}
+
+namespace {
+uint16_t bf16_rne(float f) { // round to nearest even, as __float2bfloat16_rn for finite values
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    const uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(r >> 16);
+}
+} // namespace
+
+int BatchRunner::schedule_gradient(const float* features, const float* targets, int n, float* grad, std::string& err) {
+    if (!features || !targets || !grad || n < 128) {
+        err = "gradient check needs at least 128 samples";
+        return MBX_E_INVALID;
+    }
+    int rc = ensure_sched(err);
+    if (rc != MBX_OK) return rc;
+    std::vector<uint16_t> xh((size_t)n * kSchedFeatures, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 24; ++k) xh[(size_t)i * kSchedFeatures + k] = bf16_rne(features[(size_t)i * 24 + k]);
+    void *dx = nullptr, *dt = nullptr, *dg = nullptr;
+    if (cudaMalloc(&dx, xh.size() * 2) != cudaSuccess || cudaMalloc(&dt, sizeof(float) * n) != cudaSuccess ||
+        cudaMalloc(&dg, sizeof(float) * SchedLayout::N) != cudaSuccess) {
+        if (dx) cudaFree(dx);
+        if (dt) cudaFree(dt);
+        err = "gradient check allocation failed";
+        return MBX_E_NOMEM;
+    }
+    cudaMemcpyAsync(dx, xh.data(), xh.size() * 2, cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(dt, targets, sizeof(float) * n, cudaMemcpyHostToDevice, st_);
+    cudaError_t e = sched_gradient(sched_, (const __nv_bfloat16*)dx, (const float*)dt, n, (float*)dg, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grad, dg, sizeof(float) * SchedLayout::N, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    cudaFree(dx);
+    cudaFree(dt);
+    cudaFree(dg);
+    return e == cudaSuccess ? MBX_OK : cuda_fail(err, "gradient check", e);
+}
+
 int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, std::string& err) {
-    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag) return MBX_OK;
+    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag && g_schedule_ == schedule_) return MBX_OK;
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     exec_ = nullptr;
@@ -109,17 +210,17 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
     cudaMemsetAsync(d_ctr_, 0, 6 * sizeof(Counters), st_);
     cudaMemsetAsync(d_view_interior_, 0, sizeof(unsigned) * nviews, st_);
-    auto tiers = [&](const ViewDesc* views, unsigned total, int c0, unsigned* vint) {
+    auto tiers = [&](const ViewDesc* views, unsigned total, int c0, unsigned* vint, const uint64_t* order) {
         BatchArgs a{};
         a.views = views;
         a.nviews = nviews;
         a.capacity = cap_samples_;
         a.view_interior = vint;
         a.cancel = cancel_flag;
-        // FP32 over all samples
+        // FP32 over all samples (in the learned order when given)
         a.total = total;
-        a.queue = nullptr;
-        a.queue_n = nullptr;
+        a.queue = order;
+        a.queue_n = order ? d_main_total_ : nullptr;
         a.ctr = d_ctr_ + c0;
         a.next_queue = d_qa_;
         launch_batch_pass(0, a, nsm, st_);
@@ -136,9 +237,16 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.next_queue = nullptr;
         launch_batch_pass(2, a, nsm, st_);
     };
-    tiers(d_probe_, probe_total, 0, d_view_interior_);
+    tiers(d_probe_, probe_total, 0, d_view_interior_, nullptr);
     launch_batch_gate(d_main_, nviews, d_view_interior_, st_);
-    tiers(d_main_, main_total, 3, nullptr);
+    if (schedule_) {
+        sched_probe_grid(d_probe_, d_main_, nviews, probe_total, st_);
+        sched_order(sched_, d_main_, nviews, main_total, nsm, d_qo_, st_);
+        tiers(d_main_, main_total, 3, nullptr, d_qo_);
+        if (schedule_ == 1) sched_train(sched_, d_main_, nviews, main_total, kSchedTrainSteps, 2e-3f, st_);
+    } else {
+        tiers(d_main_, main_total, 3, nullptr, nullptr);
+    }
     cudaMemcpyAsync(h_ctr_, d_ctr_, 6 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
     e = cudaStreamEndCapture(st_, &graph_);
     if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
@@ -148,6 +256,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     g_probe_ = probe_total;
     g_main_ = main_total;
     g_cancel_ = cancel_flag;
+    g_schedule_ = schedule_;
     return MBX_OK;
 }
 
@@ -160,6 +269,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
     if (rc != MBX_OK) return rc;
     std::vector<BatchSlot> slots(n);
     std::vector<mbx_stats> vst(n);
+    for (int i = 0; i < n; ++i) slots[i].want_cost = schedule_ != 0;
     for (int i = 0; i < n; ++i) {
         rc = eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
         if (rc != MBX_OK) {
@@ -196,6 +306,14 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             cudaError_t e = cudaStreamSynchronize(eng_[deferred[k]]->stream());
             if (e != cudaSuccess) return cuda_fail(err, "batch preparation", e);
         }
+        if (schedule_)
+            for (int k = 0; k < nv; ++k)
+                if (!h_desc_[k].f.out.cost || !h_desc_[nv + k].pgrid) {
+                    err = "scheduling buffers could not be allocated";
+                    return MBX_E_NOMEM;
+                }
+        h_main_total_ = main_total;
+        cudaMemcpyAsync(d_main_total_, &h_main_total_, sizeof(unsigned), cudaMemcpyHostToDevice, st_);
         cudaMemcpyAsync(d_probe_, h_desc_, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
         cudaMemcpyAsync(d_main_, h_desc_ + nv, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
         rc = build_graph(nv, probe_total, main_total, cancel_flag, err);

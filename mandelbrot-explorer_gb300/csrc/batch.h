@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "order_model.h"
 
 namespace mbx {
 
@@ -21,6 +22,11 @@ class BatchRunner {
     int run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats, volatile int* cancel_flag, std::string& err);
     void cancel();
     void reset_cancel();
+    // 1: order each batch's main pass by the learned cost model and train it on
+    // the batch's costs; 2: order with the model as it stands; 0: natural order
+    int set_schedule(int mode, std::string& err);
+    int schedule_params(const float* set, float* get, std::string& err);
+    int schedule_gradient(const float* features, const float* targets, int n, float* grad, std::string& err);
 
   private:
     int ensure_engines(int n, std::string& err);
@@ -46,6 +52,15 @@ class BatchRunner {
     int g_views_ = -1;
     unsigned g_probe_ = 0, g_main_ = 0;
     volatile int* g_cancel_ = nullptr;
+    int g_schedule_ = -1;
+    // learned ordering
+    int schedule_ = 0;
+    SchedState sched_{};
+    bool sched_ready_ = false;
+    uint64_t* d_qo_ = nullptr;       // ordered main-pass queue
+    unsigned* d_main_total_ = nullptr;
+    unsigned h_main_total_ = 0;
+    int ensure_sched(std::string& err);
 };
 
 } // namespace mbx

@@ -43,6 +43,10 @@ int validate(const mbx_request* r, std::string& why) {
     else return MBX_OK;
     return MBX_E_INVALID;
 }
+mbx::BatchRunner* batch_of(mbx_context* c) {
+    if (!c->batch) c->batch = new (std::nothrow) mbx::BatchRunner(c->engine->device());
+    return c->batch;
+}
 } // namespace
 
 extern "C" {
@@ -94,8 +98,7 @@ int mbx_compute_batch(mbx_context* c, const mbx_request* reqs, int n, mbx_stats*
     std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
     if (!busy.owns_lock()) return MBX_E_BUSY;
     std::lock_guard<std::mutex> g(g_gmp_mutex);
-    if (!c->batch) c->batch = new (std::nothrow) mbx::BatchRunner(c->engine->device());
-    if (!c->batch) return MBX_E_NOMEM;
+    if (!batch_of(c)) return MBX_E_NOMEM;
     std::string err;
     int rc = c->batch->run(reqs, n, view_stats, batch_stats, c->engine->device_cancel_flag(), err);
     c->last_error = rc == MBX_OK ? std::string() : (err.empty() ? std::string("batch failed") : err);
@@ -117,6 +120,42 @@ int mbx_compute(mbx_context* c, const mbx_request* r, mbx_stats* stats) {
     int rc = c->engine->compute(*r, stats);
     c->last_error = rc == MBX_OK ? std::string() : (c->engine->error().empty() ? std::string("compute failed") : c->engine->error());
     if (rc == MBX_E_CANCELLED) c->last_error = "cancelled";
+    return rc;
+}
+
+int mbx_set_batch_scheduling(mbx_context* c, int mode) {
+    if (!c) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::BatchRunner* b = batch_of(c);
+    if (!b) return MBX_E_NOMEM;
+    std::string err;
+    int rc = b->set_schedule(mode, err);
+    c->last_error = err;
+    return rc;
+}
+
+int mbx_schedule_params(mbx_context* c, const float* set, float* get) {
+    if (!c || (!set && !get)) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::BatchRunner* b = batch_of(c);
+    if (!b) return MBX_E_NOMEM;
+    std::string err;
+    int rc = b->schedule_params(set, get, err);
+    c->last_error = err;
+    return rc;
+}
+
+int mbx_schedule_gradient(mbx_context* c, const float* features, const float* targets, int n, float* grad) {
+    if (!c) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::BatchRunner* b = batch_of(c);
+    if (!b) return MBX_E_NOMEM;
+    std::string err;
+    int rc = b->schedule_gradient(features, targets, n, grad, err);
+    c->last_error = err;
     return rc;
 }
 

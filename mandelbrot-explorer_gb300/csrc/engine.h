@@ -74,6 +74,7 @@ int find_nucleus_disk(const char* cre, const char* cim, const char* radius, int 
 // runs those passes for all its frames in shared launches.
 struct BatchSlot {
     bool deferred = false;
+    bool want_cost = false; // learned ordering: per-sample costs and the probe grid
     ViewDesc probe, main;
 };
 
@@ -167,7 +168,7 @@ class Engine {
     mpf_t zre_[2], zim_[2];
     bool use_fixed_ = false;
     int fixL_ = 0;
-    std::vector<uint64_t> ftmp_;
+    std::vector<uint64_t> ftmp_, ftmp2_;
     FixedReal fc_re_, fc_im_, fz_re_[2], fz_im_[2], ft1_, ft2_, fab_, fre_, fim_;
     FE dfe_r_{1.0, 0}, dfe_i_{0.0, 0};
 
@@ -216,6 +217,8 @@ class Engine {
     DevBuf<Bla64> dbla64_;
     DevBuf<BlaDF> dbladf_;
     DevBuf<df2> dZdf_;
+    DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample lane cost
+    DevBuf<float2> dpgrid_;   // and the probe pass's cost per 8x8 cell
     DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
     DevBuf<uint64_t> drerun2_keys_;           // double-float pass: queue for the FP64 pass
     DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position

@@ -104,6 +104,7 @@ struct Outputs {
     double* glitch;  // per list entry glitch score (double path), -1 none
     uint8_t* done;   // per list entry: 1 finished, 0 pending
     uint8_t* gmp;    // per list entry: needs the arbitrary-precision recompute
+    uint32_t* cost = nullptr; // lane passes: per sample (getIndex layout, sub 1) lane steps + 4 per BLA skip
 };
 
 struct Counters {
@@ -217,6 +218,8 @@ struct ViewDesc {
     unsigned base;           // first batch-wide sample index of this view
     unsigned count;          // samples of this view in the pass
     int interior_gate;       // main pass: interior detection follows the probe's interior count
+    float2* pgrid;           // learned ordering: probe-pass cost and interior flag per 8x8 cell
+    int pgw, pgh;
 };
 
 // Batch-wide pass arguments. Queue entries are sample keys with the view index

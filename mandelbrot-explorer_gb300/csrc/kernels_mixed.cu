@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
+    unsigned cost0 = 0;
     bool live = false, exhausted = false, stop = false;
     unsigned rounds = 0;
     for (;;) {
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
                 const int i = base + __popc(idle & ((1u << lane_id) - 1u));
                 if (i < n && !stop) {
                     lane_setup(L, i, f, p, dxf, dyf, orb);
+                    cost0 = (unsigned)(n_steps + 4 * n_bla);
                     live = true;
                 }
             }
@@ -130,6 +132,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         if (live) {
             T zrad = T(0);
             const int st = lane_run(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase);
+            if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 // smooth value N - log2(log2|z|) in the lane type (the output is FP32)
                 f.out.iter[L.oidx] = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
@@ -210,6 +213,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
     int view = 0;
+    unsigned cost0 = 0;
     bool live = false, exhausted = false, stop = false;
     unsigned rounds = 0;
     for (;;) {
@@ -241,6 +245,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
                     }
                     const ViewDesc& vd = a.views[v];
                     lane_setup_at(L, (int)g, arr, vd.p, te_from_fe<T>(vd.p.dxfe), te_from_fe<T>(vd.p.dyfe), ViewTables<T>::orb(vd));
+                    cost0 = (unsigned)(n_steps + 4 * n_bla);
                     view = v;
                     live = true;
                 }
@@ -253,6 +258,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
             T zrad = T(0);
             const int st = lane_run(L, 32, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, (T)vd.p.g.ESC2, (1 << vd.f.bla.minlevel) - 1, zrad,
                                     n_steps, n_bla, n_skip, n_rebase);
+            if (st != 0 && vd.f.out.cost) vd.f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 vd.f.out.iter[L.oidx] = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
                 if (vd.f.out.escN) vd.f.out.escN[L.oidx] = L.iter;

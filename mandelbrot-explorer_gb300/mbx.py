@@ -128,7 +128,12 @@ EXPORTS = (
     "mbx_set_tuning",
     "mbx_autotune",
     "mbx_compute_batch",
+    "mbx_set_batch_scheduling",
+    "mbx_schedule_params",
+    "mbx_schedule_gradient",
 )
+
+SCHED_PARAMS = 64 * 24 + 64 + 64 * 64 + 64 + 64 + 1
 
 _lib = None
 _lib_lock = threading.Lock()
@@ -166,6 +171,12 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
         lib.mbx_autotune.restype = ctypes.c_int
         lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
+        lib.mbx_set_batch_scheduling.restype = ctypes.c_int
+        lib.mbx_set_batch_scheduling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.mbx_schedule_params.restype = ctypes.c_int
+        lib.mbx_schedule_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        lib.mbx_schedule_gradient.restype = ctypes.c_int
+        lib.mbx_schedule_gradient.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         lib.mbx_compute_batch.restype = ctypes.c_int
         lib.mbx_compute_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.c_int, ctypes.POINTER(Stats), ctypes.POINTER(Stats)]
         lib.mbx_render_shallow_noalloc.restype = ctypes.c_int
@@ -354,6 +365,32 @@ class CudaComputeBackend:
     def compute(self, req: ComputeRequest) -> bool:
         """True on success, like IComputeBackend::compute."""
         return self.compute_status(req) == OK
+
+    def set_batch_scheduling(self, mode: int) -> int:
+        """Learned ordering of the batched main pass: 1 on, 0 off."""
+        return self._lib.mbx_set_batch_scheduling(self._ctx, int(mode))
+
+    def schedule_params(self, set_params=None) -> np.ndarray:
+        """Reads (and first sets, when given) the ordering model's parameters."""
+        out = np.empty(SCHED_PARAMS, np.float32)
+        src = None
+        if set_params is not None:
+            src = np.ascontiguousarray(set_params, dtype=np.float32)
+            assert src.size == SCHED_PARAMS
+        rc = self._lib.mbx_schedule_params(self._ctx, src.ctypes.data if src is not None else None, out.ctypes.data)
+        if rc != OK:
+            raise RuntimeError("schedule_params failed (%d): %s" % (rc, self.last_error()))
+        return out
+
+    def schedule_gradient(self, features, targets) -> np.ndarray:
+        """Gradients of one training step of the ordering model (no update)."""
+        x = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(SCHED_PARAMS, np.float32)
+        rc = self._lib.mbx_schedule_gradient(self._ctx, x.ctypes.data, t.ctypes.data, int(t.size), g.ctypes.data)
+        if rc != OK:
+            raise RuntimeError("schedule_gradient failed (%d): %s" % (rc, self.last_error()))
+        return g
 
     def compute_batch(self, reqs) -> int:
         """Renders several frames with shared passes (mbx_compute_batch).
