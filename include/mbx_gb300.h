@@ -180,6 +180,62 @@ int mbx_render_shallow_noalloc(double c0_re, double c0_im, double dx, double dy,
                                double bailout, int coloring_method, float* iterations, int32_t* escape_iteration,
                                float* normal, void* stream);
 
+/* ---- Image epilogue: the reference's render tool (src/tools/render.cpp) ----
+ * Value -> palette coordinate (getColor, render.cpp:71-92): */
+#define MBX_MAP_LOG_POWER 0 /* powf(logf(v+2), logf(v+2)^2 * density/3600) (color_func, render.cpp:31-33) */
+#define MBX_MAP_DISTANCE 1  /* tanhf(v * density/3600 * 5): exterior distance values (MANDEL_EDE) */
+#define MBX_MAP_STRIPE 2    /* v * (density/20): stripe-average values (MANDEL_SAC) */
+#define MBX_MAP_TRAP 3      /* v: orbit-trap values are palette coordinates (MANDEL_TRAP) */
+/* Per-sample shade (render.cpp:255-292): */
+#define MBX_SHADE_NONE 0
+#define MBX_SHADE_RELIEF 1     /* screen-space slope of the values, Lambert (reliefShadeAt, render.cpp:47-69) */
+#define MBX_SHADE_NORMAL_MAP 2 /* Lambert from a normal-angle buffer (MANDEL_NORMAL, render.cpp:276-287) */
+#define MBX_SHADE_DE_OVERLAY 3 /* black-and-white filament layer from a distance buffer (render.cpp:263-274) */
+
+typedef struct {
+    int supersample;          /* ss: each output pixel averages ss x ss values in linear light */
+    int mapping;              /* MBX_MAP_* */
+    int shading;              /* MBX_SHADE_* */
+    float density;            /* colour density (color_density, render.cpp:21; MANDEL_DENS) */
+    double light_az, light_el; /* light direction in radians (render.cpp:45; MANDEL_LIGHT_AZ/EL) */
+    double relief_strength;   /* slope strength (MANDEL_RELIEF_STR) */
+    double de_k;              /* overlay falloff (MANDEL_DE_K) */
+} mbx_color_params;
+
+/* The render tool's defaults: ss 1, log-power mapping, no shading, density 60,
+ * light (2.3, 0.55), relief strength 1, overlay falloff 1.5. */
+void mbx_color_defaults(mbx_color_params* p);
+
+/* Colours (width*ss) x (height*ss) values (the iterations output of a render)
+ * into rgb[height][width][3] (render.cpp:248-300). aux is the normal-angle or
+ * distance buffer of the same layout for those shadings, else NULL. With
+ * on_device = 1 values, aux and rgb are CUDA device pointers and nothing is
+ * copied; otherwise they are host pointers. Runs on the context's stream and
+ * returns when the image is complete. */
+int mbx_colorize(mbx_context* ctx, const mbx_color_params* p, const float* values, const float* aux, int width, int height,
+                 int on_device, uint8_t* rgb);
+
+/* Render and colour in one call, the render tool's pipeline without its host
+ * colouring loop: the frame (req: sub 1, width and height multiples of
+ * p->supersample; its output pointers are ignored) is computed into
+ * context-owned device buffers, coloured there, and only the
+ * (width/ss) x (height/ss) RGB image is copied to rgb (host). The distance
+ * overlay takes its buffer from MBX_DE_OVERLAY in req->coloring_method. */
+int mbx_render_image(mbx_context* ctx, const mbx_request* req, const mbx_color_params* p, uint8_t* rgb, mbx_stats* stats);
+
+/* Device time of the last colour pass (CUDA events on the context's stream)
+ * and how many palette coordinates took the FP64 path (see mbx_colorize). */
+int mbx_last_color_stats(const mbx_context* ctx, double* gpu_ms, long long* fp64_fallbacks);
+
+/* writeBMP (render.cpp:101-137): 24-bit BMP, bottom-up BGR rows padded to 4
+ * bytes. Host only. */
+int mbx_write_bmp(const char* path, const uint8_t* rgb, int width, int height);
+
+/* The epilogue's host-built tables, for inspection: the palette as three
+ * 2048-entry channels (render.cpp:23-29), and the 352 gamma thresholds
+ * (least linear value giving each encoded value 1..352). Host only. */
+void mbx_color_tables(float* palette, float* gamma_thresholds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,7 @@ def units():
         ("kernels_mixed.o", [NVCC] + common_nv + ["-fmad=true", "-c", os.path.join(SRC, "kernels_mixed.cu")]),
         ("noalloc.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "noalloc.cu")]),
         ("order_model.o", [NVCC] + common_nv + ["-fmad=true", "-c", os.path.join(SRC, "order_model.cu")]),
+        ("color.o", [NVCC] + common_nv + ["-fmad=false", "-c", os.path.join(SRC, "color.cu")]),
         ("engine.o", cxx + ["-c", os.path.join(SRC, "engine.cpp")]),
         ("capi.o", cxx + ["-c", os.path.join(SRC, "capi.cpp")]),
         ("batch.o", cxx + ["-c", os.path.join(SRC, "batch.cpp")]),

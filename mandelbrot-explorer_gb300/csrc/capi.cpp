@@ -8,11 +8,15 @@
 #include <string>
 
 #include "batch.h"
+#include "color.h"
 #include "engine.h"
 
 struct mbx_context {
     mbx::Engine* engine = nullptr;
     mbx::BatchRunner* batch = nullptr;
+    mbx::Colorizer* color = nullptr;
+    double color_gpu_ms = 0.0;
+    long long color_fallbacks = 0;
     std::string name = "cuda";
     std::string detail;
     std::string last_error;
@@ -47,6 +51,10 @@ mbx::BatchRunner* batch_of(mbx_context* c) {
     if (!c->batch) c->batch = new (std::nothrow) mbx::BatchRunner(c->engine->device());
     return c->batch;
 }
+mbx::Colorizer* color_of(mbx_context* c) {
+    if (!c->color) c->color = new (std::nothrow) mbx::Colorizer();
+    return c->color;
+}
 } // namespace
 
 extern "C" {
@@ -80,6 +88,7 @@ mbx_context* mbx_create(int device, char* err, int err_len) {
 void mbx_destroy(mbx_context* c) {
     if (!c) return;
     delete c->batch;
+    delete c->color;
     delete c->engine;
     delete c;
 }
@@ -255,6 +264,139 @@ int mbx_find_nucleus(const char* center_re, const char* center_im, const char* r
         memcpy(nucleus_im, b.c_str(), b.size() + 1);
     }
     return p;
+}
+
+void mbx_color_defaults(mbx_color_params* p) { // render.cpp:21, 44-46
+    if (!p) return;
+    p->supersample = 1;
+    p->mapping = MBX_MAP_LOG_POWER;
+    p->shading = MBX_SHADE_NONE;
+    p->density = 60.0f;
+    p->light_az = 2.3;
+    p->light_el = 0.55;
+    p->relief_strength = 1.0;
+    p->de_k = 1.5;
+}
+
+int mbx_colorize(mbx_context* c, const mbx_color_params* p, const float* values, const float* aux, int width, int height, int on_device, uint8_t* rgb) {
+    if (!c) return MBX_E_INVALID;
+    std::string why;
+    if (mbx::validate_color_params(p, why) != MBX_OK) {
+        std::lock_guard<std::mutex> l(c->mu);
+        c->last_error = why;
+        return MBX_E_INVALID;
+    }
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::Colorizer* col = color_of(c);
+    if (!col) return MBX_E_NOMEM;
+    unsigned fb = 0;
+    float ms = 0.0f;
+    std::string err;
+    const int rc = col->colorize(*p, values, aux, width, height, on_device != 0, rgb, c->engine->stream(), c->engine->sm_count(), err, &fb, &ms);
+    c->last_error = err;
+    if (rc == MBX_OK) {
+        c->color_gpu_ms = ms;
+        c->color_fallbacks = fb;
+    }
+    return rc;
+}
+
+int mbx_render_image(mbx_context* c, const mbx_request* r, const mbx_color_params* p, uint8_t* rgb, mbx_stats* stats) {
+    if (!c || !r || !rgb) return MBX_E_INVALID;
+    std::string why;
+    mbx_request q = *r;
+    float dummy = 0.0f;
+    if (!q.iterations) q.iterations = &dummy; // replaced below; validate() wants a buffer
+    int v = validate(&q, why);
+    if (v == MBX_OK) v = mbx::validate_color_params(p, why);
+    if (v == MBX_OK) {
+        if (r->sub != 1) why = "render_image takes sub 1 (supersampling is the colour pass's ss)";
+        else if (r->width % p->supersample || r->height % p->supersample) why = "width and height must be multiples of supersample";
+        else if (p->shading == MBX_SHADE_NORMAL_MAP) why = "normal-map shading needs a normal-angle buffer the renderer does not produce; use mbx_colorize";
+        else if (p->shading == MBX_SHADE_DE_OVERLAY && !(r->coloring_method & MBX_DE_OVERLAY)) why = "distance-overlay shading needs MBX_DE_OVERLAY in coloring_method";
+        v = why.empty() ? MBX_OK : MBX_E_INVALID;
+    }
+    if (v != MBX_OK) {
+        std::lock_guard<std::mutex> l(c->mu);
+        c->last_error = why;
+        return v;
+    }
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::Colorizer* col = color_of(c);
+    if (!col) return MBX_E_NOMEM;
+    const int ow = r->width / p->supersample, oh = r->height / p->supersample;
+    const size_t samples = (size_t)r->width * r->height, pixels = (size_t)ow * oh;
+    const bool need_aux = p->shading == MBX_SHADE_DE_OVERLAY;
+    float *dv = nullptr, *da = nullptr;
+    uint8_t* drgb = nullptr;
+    std::string err;
+    int rc = col->device_buffers(samples, pixels, need_aux, &dv, &da, &drgb, err);
+    if (rc != MBX_OK) {
+        c->last_error = err;
+        return rc;
+    }
+    q.outputs_on_device = 1;
+    q.iterations = dv;
+    q.normal = (r->coloring_method & MBX_DE_OVERLAY) ? da : nullptr;
+    if ((r->coloring_method & MBX_DE_OVERLAY) && !da) {
+        // the overlay buffer is computed even when the chosen shading ignores it
+        rc = col->device_buffers(samples, pixels, true, &dv, &da, &drgb, err);
+        if (rc != MBX_OK) {
+            c->last_error = err;
+            return rc;
+        }
+        q.iterations = dv;
+        q.normal = da;
+    }
+    q.escape_iteration = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_gmp_mutex);
+        rc = c->engine->compute(q, stats);
+    }
+    if (rc != MBX_OK) {
+        c->last_error = c->engine->error().empty() ? std::string("compute failed") : c->engine->error();
+        if (rc == MBX_E_CANCELLED) c->last_error = "cancelled";
+        return rc;
+    }
+    unsigned fb = 0;
+    float ms = 0.0f;
+    rc = col->colorize(*p, dv, da, ow, oh, true, drgb, c->engine->stream(), c->engine->sm_count(), err, &fb, &ms);
+    if (rc == MBX_OK) {
+        const cudaError_t e = cudaMemcpyAsync(rgb, drgb, pixels * 3, cudaMemcpyDeviceToHost, c->engine->stream());
+        const cudaError_t e2 = e == cudaSuccess ? cudaStreamSynchronize(c->engine->stream()) : e;
+        if (e2 != cudaSuccess) {
+            err = std::string("image copy: ") + cudaGetErrorString(e2);
+            rc = MBX_E_CUDA;
+        }
+    }
+    c->last_error = err;
+    if (rc == MBX_OK) {
+        c->color_gpu_ms = ms;
+        c->color_fallbacks = fb;
+    }
+    return rc;
+}
+
+int mbx_last_color_stats(const mbx_context* c, double* gpu_ms, long long* fp64_fallbacks) {
+    if (!c) return MBX_E_INVALID;
+    if (gpu_ms) *gpu_ms = c->color_gpu_ms;
+    if (fp64_fallbacks) *fp64_fallbacks = c->color_fallbacks;
+    return MBX_OK;
+}
+
+int mbx_write_bmp(const char* path, const uint8_t* rgb, int width, int height) { return mbx::write_bmp(path, rgb, width, height); }
+
+void mbx_color_tables(float* palette, float* gamma_thresholds) {
+    if (palette) mbx::build_palette(palette);
+    if (gamma_thresholds) {
+        mbx::ColorTables* t = new (std::nothrow) mbx::ColorTables();
+        if (!t) return;
+        mbx::build_color_tables(*t);
+        memcpy(gamma_thresholds, t->gamma, sizeof(t->gamma));
+        delete t;
+    }
 }
 
 } // extern "C"

@@ -131,7 +131,40 @@ EXPORTS = (
     "mbx_set_batch_scheduling",
     "mbx_schedule_params",
     "mbx_schedule_gradient",
+    "mbx_color_defaults",
+    "mbx_colorize",
+    "mbx_render_image",
+    "mbx_last_color_stats",
+    "mbx_write_bmp",
+    "mbx_color_tables",
 )
+
+# Image epilogue (render.cpp colouring): value mappings and shadings.
+MAP_LOG_POWER, MAP_DISTANCE, MAP_STRIPE, MAP_TRAP = 0, 1, 2, 3
+SHADE_NONE, SHADE_RELIEF, SHADE_NORMAL_MAP, SHADE_DE_OVERLAY = 0, 1, 2, 3
+GAMMA_STEPS = 352
+
+
+class ColorParams(ctypes.Structure):
+    """mbx_color_params; defaults are the render tool's (render.cpp:21, 44-46)."""
+
+    _fields_ = [
+        ("supersample", ctypes.c_int),
+        ("mapping", ctypes.c_int),
+        ("shading", ctypes.c_int),
+        ("density", ctypes.c_float),
+        ("light_az", ctypes.c_double),
+        ("light_el", ctypes.c_double),
+        ("relief_strength", ctypes.c_double),
+        ("de_k", ctypes.c_double),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__(1, MAP_LOG_POWER, SHADE_NONE, 60.0, 2.3, 0.55, 1.0, 1.5)
+        for k, v in kw.items():
+            if k not in dict(self._fields_):
+                raise TypeError("unknown colour parameter %r" % k)
+            setattr(self, k, v)
 
 SCHED_PARAMS = 64 * 24 + 64 + 64 * 64 + 64 + 64 + 1
 
@@ -183,6 +216,16 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_render_shallow_noalloc.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int] * 3 + [ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 4
         lib.mbx_find_nucleus.restype = ctypes.c_int
         lib.mbx_find_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.mbx_color_defaults.argtypes = [ctypes.POINTER(ColorParams)]
+        lib.mbx_colorize.restype = ctypes.c_int
+        lib.mbx_colorize.argtypes = [ctypes.c_void_p, ctypes.POINTER(ColorParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        lib.mbx_render_image.restype = ctypes.c_int
+        lib.mbx_render_image.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(ColorParams), ctypes.c_void_p, ctypes.POINTER(Stats)]
+        lib.mbx_last_color_stats.restype = ctypes.c_int
+        lib.mbx_last_color_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]
+        lib.mbx_write_bmp.restype = ctypes.c_int
+        lib.mbx_write_bmp.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.mbx_color_tables.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         if path is None:
             _lib = lib
         return lib
@@ -392,6 +435,49 @@ class CudaComputeBackend:
             raise RuntimeError("schedule_gradient failed (%d): %s" % (rc, self.last_error()))
         return g
 
+    def colorize(self, values, width: int, height: int, params: "ColorParams" = None, aux=None, rgb=None):
+        """mbx_colorize: values (width*ss x height*ss, numpy or CUDA tensor) -> RGB [height][width][3].
+        Device tensors in give a device tensor out (nothing copied)."""
+        p = params or ColorParams()
+        vp, dev = self._ptr(values)
+        ap, adev = self._ptr(aux)
+        if aux is not None and adev != dev:
+            raise ValueError("values and aux must both be host arrays or both CUDA tensors")
+        if rgb is None:
+            if dev:
+                import torch
+
+                rgb = torch.empty((height, width, 3), dtype=torch.uint8, device=values.device)
+            else:
+                rgb = np.empty((height, width, 3), np.uint8)
+        op, odev = self._ptr(rgb)
+        if odev != dev:
+            raise ValueError("rgb must live where values live")
+        rc = self._lib.mbx_colorize(self._ctx, ctypes.byref(p), vp, ap, width, height, 1 if dev else 0, op)
+        if rc != OK:
+            raise RuntimeError("mbx_colorize failed (%d): %s" % (rc, self.last_error()))
+        return rgb
+
+    def render_image(self, req: "ComputeRequest", params: "ColorParams" = None) -> np.ndarray:
+        """mbx_render_image: compute + colour on the device; returns the RGB image (host)."""
+        p = params or ColorParams()
+        r, _keep = self._build(req)
+        ss = p.supersample
+        out = np.empty((req.height // ss, req.width // ss, 3), np.uint8)
+        st = Stats()
+        rc = self._lib.mbx_render_image(self._ctx, ctypes.byref(r), ctypes.byref(p), out.ctypes.data, ctypes.byref(st))
+        self.last_stats = st
+        if rc != OK:
+            raise RuntimeError("mbx_render_image failed (%d): %s" % (rc, self.last_error()))
+        return out
+
+    def last_color_stats(self):
+        """(device ms of the last colour pass, palette coordinates that took the FP64 path)."""
+        ms = ctypes.c_double(0.0)
+        fb = ctypes.c_longlong(0)
+        self._lib.mbx_last_color_stats(self._ctx, ctypes.byref(ms), ctypes.byref(fb))
+        return ms.value, fb.value
+
     def compute_batch(self, reqs) -> int:
         """Renders several frames with shared passes (mbx_compute_batch).
         Sets last_view_stats (one Stats per frame) and last_batch_stats."""
@@ -404,6 +490,24 @@ class CudaComputeBackend:
         self.last_batch_stats = bst
         self.last_status = rc
         return rc
+
+
+def write_bmp(path: str, rgb) -> None:
+    """render.cpp's writeBMP for an RGB image [height][width][3] (uint8). Host only."""
+    img = np.ascontiguousarray(rgb, np.uint8)
+    if img.ndim != 3 or img.shape[2] != 3:
+        raise ValueError("rgb must be [height][width][3]")
+    rc = load_library().mbx_write_bmp(path.encode(), img.ctypes.data, img.shape[1], img.shape[0])
+    if rc != OK:
+        raise OSError("mbx_write_bmp failed (%d)" % rc)
+
+
+def color_tables():
+    """(palette float32 [3][2048], gamma thresholds float32 [352]) as built on this host."""
+    pal = np.empty((3, 2048), np.float32)
+    thr = np.empty(GAMMA_STEPS, np.float32)
+    load_library().mbx_color_tables(pal.ctypes.data, thr.ctypes.data)
+    return pal, thr
 
 
 def create_compute_backend(requested: str = "cuda", device: int = 0) -> CudaComputeBackend:

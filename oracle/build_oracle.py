@@ -1,6 +1,6 @@
 """Build recipe for the oracle (test infrastructure only).
 
-Compiles oracle/mbx_oracle.cpp into oracle/lib/libmbx_oracle.so with
+Compiles oracle/mbx_oracle.cpp and oracle/mbx_color.cpp into oracle/lib/libmbx_oracle.so with
 -ffp-contract=off (the restated operation order must be the executed order on
 every host, x86-64 and aarch64 alike) and, when the reference sources are
 present, the reference engine itself into oracle/_ref/ via ref_build/Makefile.
@@ -24,12 +24,12 @@ def find_libgmp():
 
 
 def build_oracle(force=False):
-    src = os.path.join(HERE, "mbx_oracle.cpp")
+    srcs = [os.path.join(HERE, "mbx_oracle.cpp"), os.path.join(HERE, "mbx_color.cpp")]
     hdr = os.path.join(HERE, "oracle_gmp.h")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in srcs + [hdr]):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", LIB, find_libgmp()]
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"] + srcs + ["-o", LIB, find_libgmp()]
     subprocess.check_call(cmd)
     return LIB
 

@@ -26,8 +26,52 @@ def load():
         lib.mbx_oracle_render.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 6 + [ctypes.c_double] + [ctypes.c_int] * 3 + [ctypes.c_void_p] * 4
         lib.mbx_oracle_truth.restype = ctypes.c_int
         lib.mbx_oracle_truth.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 7 + [ctypes.c_double] + [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.mbx_oracle_colorize.restype = ctypes.c_int
+        lib.mbx_oracle_colorize.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 5 + [ctypes.c_float] + [ctypes.c_double] * 4 + [ctypes.c_void_p]
+        lib.mbx_oracle_bmp.restype = ctypes.c_long
+        lib.mbx_oracle_bmp.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        lib.mbx_oracle_palette.argtypes = [ctypes.c_void_p]
+        lib.mbx_oracle_gamma_value.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         _lib = lib
     return _lib
+
+
+def palette():
+    """The reference's 2048-entry palette as float32 [3][2048] (render.cpp:23-29)."""
+    m = np.empty((3, 2048), np.float32)
+    load().mbx_oracle_palette(m.ctypes.data)
+    return m
+
+
+def colorize(values, width, height, ss=1, aux=None, mapping=0, shading=0, density=60.0, light_az=2.3, light_el=0.55, relief_strength=1.0, de_k=1.5):
+    """render.cpp's colouring + ss x ss linear-light downsample: uint8 [height][width][3]."""
+    v = np.ascontiguousarray(values, np.float32).ravel()
+    if v.size != width * height * ss * ss:
+        raise ValueError("values must hold (width*ss) x (height*ss) samples")
+    a = None if aux is None else np.ascontiguousarray(aux, np.float32).ravel()
+    out = np.empty((height, width, 3), np.uint8)
+    rc = load().mbx_oracle_colorize(v.ctypes.data, None if a is None else a.ctypes.data, width, height, ss, mapping, shading, float(density), float(light_az), float(light_el), float(relief_strength), float(de_k), out.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle rejected the colour parameters")
+    return out
+
+
+def gamma_value(l):
+    """(int)(255 powf(l, 1/2.2) + 0.5) per linear value, as render.cpp encodes a channel."""
+    l = np.ascontiguousarray(l, np.float32).ravel()
+    out = np.empty(l.size, np.int32)
+    load().mbx_oracle_gamma_value(l.ctypes.data, l.size, out.ctypes.data)
+    return out
+
+
+def bmp_bytes(rgb):
+    """render.cpp's 24-bit BMP file for an RGB image [height][width][3]."""
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    h, w = rgb.shape[:2]
+    n = load().mbx_oracle_bmp(None, w, h, None)
+    buf = np.empty(n, np.uint8)
+    load().mbx_oracle_bmp(rgb.ctypes.data, w, h, buf.ctypes.data)
+    return buf.tobytes()
 
 
 def precision_for_scale(scale):

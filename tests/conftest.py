@@ -34,3 +34,28 @@ def load_fixture(name, case):
 @pytest.fixture(scope="session")
 def cases():
     return load_cases()
+
+
+def load_color_cases():
+    with open(os.path.join(GOLDEN, "color_cases.json")) as f:
+        return json.load(f)
+
+
+def load_color_fixture(name, case):
+    """(values, aux or None, reference BMP bytes) of an image-epilogue case."""
+    n = case["width"] * case["height"] * case["ss"] ** 2
+    a = np.fromfile(os.path.join(GOLDEN, "color_%s.f32" % name), dtype="<f4")
+    with open(os.path.join(GOLDEN, "color_%s.bmp" % name), "rb") as f:
+        bmp = f.read()
+    return a[:n], (a[n:] if a.size > n else None), bmp
+
+
+def bmp_rgb(bmp, width, height):
+    """RGB [height][width][3] of a bottom-up 24-bit BMP."""
+    row = (width * 3 + 3) & ~3
+    data = np.frombuffer(bmp, np.uint8, offset=54).reshape(height, row)[::-1, : width * 3]
+    return data.reshape(height, width, 3)[:, :, ::-1].copy()
+
+
+def color_kwargs(case):
+    return {k: case[k] for k in ("mapping", "shading", "density", "light_az", "light_el", "relief_strength", "de_k")}
