@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 
 namespace mbx {
@@ -677,7 +678,252 @@ static void sqadd(mpf_ptr zr, mpf_ptr zi, mpf_srcptr cr, mpf_srcptr ci, mpf_ptr 
     mpf_add(zi, zi, ci);
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined forms of the period search and the Newton orbit for precisions
+// where one product takes a fraction of a microsecond (below kParBits6 /
+// kParBits4): a parallel round's synchronisation would cost as much as the
+// products it overlaps. Instead the loop's independent recurrences run on
+// their own threads, linked by ring buffers and progress counters: the orbit
+// z -> z^2 + c runs ahead while the derivative (Newton) or the disk radius and
+// the containment test (period search) follow it. Every value is produced by
+// the same GMP calls, in the same order, into variables of the same precision
+// as in the serial loop, so the results are bit for bit the same.
+namespace {
+
+constexpr int kRing = 64; // iterates kept between the leading and trailing threads
+// Below this a product takes under ~0.2 us and the threads' hand-offs (a
+// ~0.28 us round trip between Neoverse V2 cores) cost what the overlap gains;
+// measured there: a 1063-bit Newton step 1.31 -> 0.87 us, 1500-bit 2.20 -> 1.06 us,
+// 700-bit no gain.
+constexpr mp_bitcnt_t kPipeMinBits = 1000;
+
+struct alignas(64) Progress {
+    std::atomic<long> v{0};
+};
+inline void wait_at_least(const Progress& p, long v, const std::atomic<bool>* stop = nullptr) {
+    while (p.v.load(std::memory_order_acquire) < v)
+        if (stop && stop->load(std::memory_order_relaxed)) return;
+}
+
+// Iterates written by one thread and read by others: each variable (its header
+// and, through a spacer allocation after it, its limbs) on cache lines of its
+// own, so that a writer never invalidates a line another thread is reading.
+struct MpfRing {
+    struct alignas(64) Slot {
+        __mpf_struct v;
+    };
+    std::vector<Slot> v;
+    std::vector<void*> spacers;
+    MpfRing(int n, mp_bitcnt_t prec) : v((size_t)n) {
+        for (auto& x : v) {
+            mpf_init2(&x.v, prec);
+            spacers.push_back(malloc(128));
+        }
+    }
+    ~MpfRing() {
+        for (auto& x : v) mpf_clear(&x.v);
+        for (void* q : spacers) free(q);
+    }
+    mpf_ptr operator[](long i) { return &v[(size_t)(i % (long)v.size())].v; }
+};
+
+// One Newton orbit z_{i+1} = z_i^2 + c, d_{i+1} = 2 z_i d_i + 1 from z_0 = d_0 = 0
+// over `period` steps, on three threads: 0 the orbit, 1 Re d, 2 Im d.
+struct NewtonPipe {
+    mpf_srcptr cr, ci;
+    long period;
+    mp_bitcnt_t prec;
+    MpfRing zr, zi, dr, di; // dr/di: two buffers (step parity)
+    Progress z_done, re_done, im_done; // z_0..z_{z_done-1}; d_1..d_{*_done}
+    NewtonPipe(mpf_srcptr c_re, mpf_srcptr c_im, long p, mp_bitcnt_t pr)
+        : cr(c_re), ci(c_im), period(p), prec(pr), zr(kRing, pr), zi(kRing, pr), dr(2, pr), di(2, pr) {}
+
+    void orbit() {
+        MpfTemp t1(prec), t2(prec), e6(prec), f7(prec);
+        for (long i = 0; i < period; ++i) {
+            // slot i+1 last held z_{i+1-kRing}, read at that step by both followers
+            wait_at_least(re_done, i + 2 - kRing);
+            wait_at_least(im_done, i + 2 - kRing);
+            mpf_srcptr a = zr[i], b = zi[i];
+            mpf_add(t1, a, b);
+            mpf_sub(t2, a, b);
+            mpf_mul(e6, a, b);
+            mpf_mul(f7, t1, t2);
+            mpf_add(zr[i + 1], f7, cr);
+            mpf_mul_ui(zi[i + 1], e6, 2);
+            mpf_add(zi[i + 1], zi[i + 1], ci);
+            z_done.v.store(i + 2, std::memory_order_release);
+        }
+    }
+    // Re d_{i+1} = 2 (zr dr - zi di) + 1
+    void real_part() {
+        MpfTemp s1(prec), s2(prec);
+        for (long i = 0; i < period; ++i) {
+            wait_at_least(z_done, i + 1);
+            wait_at_least(im_done, i); // Im d_i, and Im's read of Re d_{i-1} is done
+            mpf_mul(s1, zr[i], dr[i]);
+            mpf_mul(s2, zi[i], di[i]);
+            mpf_ptr out = dr[i + 1];
+            mpf_sub(out, s1, s2);
+            mpf_mul_ui(out, out, 2);
+            mpf_add_ui(out, out, 1);
+            re_done.v.store(i + 1, std::memory_order_release);
+        }
+    }
+    // Im d_{i+1} = 2 (zr di + zi dr)
+    void imag_part() {
+        MpfTemp c4(prec), c5(prec);
+        for (long i = 0; i < period; ++i) {
+            wait_at_least(z_done, i + 1);
+            wait_at_least(re_done, i);
+            mpf_mul(c4, zr[i], di[i]);
+            mpf_mul(c5, zi[i], dr[i]);
+            mpf_ptr out = di[i + 1];
+            mpf_add(out, c4, c5);
+            mpf_mul_ui(out, out, 2);
+            im_done.v.store(i + 1, std::memory_order_release);
+        }
+    }
+    static void run_part(void* ctx, int k) {
+        NewtonPipe* p = static_cast<NewtonPipe*>(ctx);
+        if (k == 0) p->orbit();
+        else if (k == 1) p->real_part();
+        else p->imag_part();
+    }
+    // z_p, d_p into the caller's variables after a full run
+    void run(mpf_ptr out_zr, mpf_ptr out_zi, mpf_ptr out_dr, mpf_ptr out_di) {
+        mpf_set_ui(zr[0], 0);
+        mpf_set_ui(zi[0], 0);
+        mpf_set_ui(dr[0], 0);
+        mpf_set_ui(di[0], 0);
+        z_done.v.store(1);
+        re_done.v.store(0);
+        im_done.v.store(0);
+        ParMul::instance().run(&NewtonPipe::run_part, this, 3);
+        mpf_set(out_zr, zr[period]);
+        mpf_set(out_zi, zi[period]);
+        mpf_set(out_dr, dr[period]);
+        mpf_set(out_di, di[period]);
+    }
+};
+
+// The period search on three threads: 0 the orbit (and |z| as a double), 1 the
+// disk radius R, 2 the containment test |z|^2 <= R^2 and the escape test.
+struct BallPipe {
+    mpf_srcptr cr, ci, r;
+    int maxp;
+    mp_bitcnt_t prec;
+    double cab;
+    const std::atomic<bool>* cancel;
+    MpfRing zr, zi, R, ru_ring;
+    std::vector<double> za; // |z_p| ring
+    std::vector<double> Rd; // R_p as a double
+    Progress z_done, r_done, q_done; // steps whose z_p / R_p / test are complete
+    std::atomic<bool> stop{false};
+    int result = 0;
+    BallPipe(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr rad, int mp, mp_bitcnt_t pr, const std::atomic<bool>* c)
+        : cr(c_re), ci(c_im), r(rad), maxp(mp), prec(pr), cancel(c), zr(kRing, pr), zi(kRing, pr), R(kRing, pr), ru_ring(1, pr),
+          za(kRing), Rd(kRing) {}
+
+    void orbit() {
+        MpfTemp s1(prec), s2(prec), s3(prec), F(prec);
+        for (long p = 1; p <= maxp; ++p) {
+            // slot p last held step p - kRing, read by the radius thread at step
+            // p - kRing + 1 (its |z|) and by the test at step p - kRing
+            wait_at_least(q_done, p - kRing, &stop);
+            wait_at_least(r_done, p - kRing + 1, &stop);
+            // past escape |z| squares each step: run ahead only while it is
+            // moderate, else take step p only once the serial loop would (the
+            // test passed step p - 1)
+            if (!(za[(size_t)((p - 1) % kRing)] < 1e300)) wait_at_least(q_done, p - 1, &stop);
+            if (stop.load(std::memory_order_relaxed)) return;
+            mpf_srcptr a = zr[p - 1], b = zi[p - 1];
+            mpf_add(s1, a, b);
+            mpf_sub(s2, a, b);
+            mpf_mul(s3, a, b);
+            mpf_mul(F, s1, s2);
+            mpf_add(zr[p], F, cr);
+            mpf_mul_ui(zi[p], s3, 2);
+            mpf_add(zi[p], zi[p], ci);
+            za[(size_t)(p % kRing)] = std::hypot(mpf_get_d(zr[p]), mpf_get_d(zi[p]));
+            z_done.v.store(p, std::memory_order_release);
+        }
+    }
+    void radius() {
+        MpfTemp t(prec), nb(prec), tq(prec);
+        mpf_srcptr ru = ru_ring[0];
+        for (long p = 1; p <= maxp; ++p) {
+            wait_at_least(z_done, p - 1, &stop);     // |z_{p-1}|
+            wait_at_least(q_done, p - kRing, &stop); // slot p of R free
+            if (stop.load(std::memory_order_relaxed)) return;
+            const double a = za[(size_t)((p - 1) % kRing)];
+            // a huge |z| (whose square or double would not convert to GMP)
+            // is only used when the serial loop reaches this step
+            if (!(a < 1e150)) {
+                wait_at_least(q_done, p - 1, &stop);
+                if (stop.load(std::memory_order_relaxed)) return;
+            }
+            mpf_set_d(t, 2.0 * a);
+            mpf_add(nb, t, R[p - 1]);
+            mpf_set_d(tq, a * a + cab + 1.0);
+            mpf_mul(nb, nb, R[p - 1]);
+            mpf_mul(tq, tq, ru);
+            mpf_add(nb, nb, r);
+            mpf_add(nb, nb, tq);
+            mpf_set(R[p], nb);
+            Rd[(size_t)(p % kRing)] = mpf_get_d(R[p]);
+            r_done.v.store(p, std::memory_order_release);
+        }
+    }
+    void test() {
+        MpfTemp s1(prec), s2(prec), R2m(prec), zabs2(prec);
+        for (long p = 1; p <= maxp; ++p) {
+            if (cancel && (p & 1023) == 0 && cancel->load()) break;
+            wait_at_least(z_done, p);
+            wait_at_least(r_done, p);
+            mpf_mul(s1, zr[p], zr[p]);
+            mpf_mul(s2, zi[p], zi[p]);
+            mpf_mul(R2m, R[p], R[p]);
+            mpf_add(zabs2, s1, s2);
+            if (mpf_cmp(zabs2, R2m) <= 0) {
+                result = (int)p;
+                break;
+            }
+            if (za[(size_t)(p % kRing)] > cab + 2.0 + Rd[(size_t)(p % kRing)]) break;
+            q_done.v.store(p, std::memory_order_release);
+        }
+        stop.store(true, std::memory_order_relaxed);
+    }
+    static void run_part(void* ctx, int k) {
+        BallPipe* b = static_cast<BallPipe*>(ctx);
+        if (k == 0) b->orbit();
+        else if (k == 1) b->radius();
+        else b->test();
+    }
+    int run() {
+        mpf_set_ui(zr[0], 0);
+        mpf_set_ui(zi[0], 0);
+        mpf_set_ui(R[0], 0);
+        cab = std::hypot(mpf_get_d(cr), mpf_get_d(ci));
+        mpf_ptr ru = ru_ring[0];
+        mpf_set_ui(ru, 1);
+        mpf_div_2exp(ru, ru, prec > 64 ? prec - 32 : prec / 2);
+        za[0] = 0.0;
+        ParMul::instance().run(&BallPipe::run_part, this, 3);
+        return result;
+    }
+};
+
+} // namespace
+
 int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_t prec, const std::atomic<bool>* cancel) {
+    if (prec >= kPipeMinBits && prec < kParBits4 && maxp >= 64) {
+        ParSession par(true);
+        if (ParMul::instance().concurrent(3)) {
+            BallPipe b(cr, ci, r, maxp, prec, cancel);
+            return b.run();
+        }
+    }
     MpfTemp s1(prec), s2(prec), s3(prec), zr(prec), zi(prec), R(prec), R2m(prec), zabs2(prec), nb(prec), ru(prec), t(prec), tq(prec), F(prec);
     ParSession par(prec >= kParBits4);
     mpf_set_ui(zr, 0);
@@ -722,7 +968,10 @@ int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_
 bool newton_nucleus(mpf_ptr cr, mpf_ptr ci, int period, mp_bitcnt_t prec, int maxit) {
     MpfTemp s1(prec), s2(prec), s3(prec), zr(prec), zi(prec), dr(prec), di(prec), den(prec), nr(prec), ni(prec), tol(prec), step2(prec);
     MpfTemp c4(prec), c5(prec), e6(prec), f7(prec), t1(prec), t2(prec);
-    ParSession par(prec >= kParBits6);
+    const bool piped = prec >= kPipeMinBits && prec < kParBits6 && period >= 64;
+    ParSession par(prec >= kParBits6 || piped);
+    std::unique_ptr<NewtonPipe> pipe;
+    if (piped && ParMul::instance().concurrent(3)) pipe.reset(new NewtonPipe(cr, ci, period, prec));
     mpf_set_ui(tol, 1);
     mpf_div_2exp(tol, tol, prec > 96 ? prec - 48 : prec / 2);
     mpf_mul(tol, tol, tol);
@@ -731,7 +980,8 @@ bool newton_nucleus(mpf_ptr cr, mpf_ptr ci, int period, mp_bitcnt_t prec, int ma
         mpf_set_ui(zi, 0);
         mpf_set_ui(dr, 0);
         mpf_set_ui(di, 0);
-        for (int i = 0; i < period; ++i) {
+        if (pipe) pipe->run(zr, zi, dr, di);
+        else for (int i = 0; i < period; ++i) {
             // dz' = 2 z dz + 1 and z' = z^2 + c: six products of the old
             // iterate, one round
             mpf_add(t1, zr, zi);

@@ -63,8 +63,10 @@ void ParMul::helper(int h) {
     }
 }
 
+bool ParMul::concurrent(int n) const { return n > 1 && n <= width() && open_.load(std::memory_order_acquire) && (long)getpid() == pid_; }
+
 void ParMul::run(Fn fn, void* ctx, int n) {
-    if (n <= 1 || n > width() || !open_.load(std::memory_order_acquire) || (long)getpid() != pid_) {
+    if (!concurrent(n)) {
         for (int k = 0; k < n; ++k) fn(ctx, k);
         return;
     }

@@ -27,6 +27,10 @@ class ParMul {
     // fn(ctx, k) for k in [0, n): k = 0 on the caller, the others on helpers.
     // Inside an open session and n <= width(); otherwise all run on the caller.
     void run(Fn fn, void* ctx, int n);
+    // True when run(.., n) will execute its n calls concurrently (an open
+    // session in the owning process with n <= width()): calls that wait on
+    // one another may only be issued then.
+    bool concurrent(int n) const;
     void open();
     void close();
     int width() const { return (int)helpers_.size() + 1; }

@@ -2321,4 +2321,41 @@ int mbx_oracle_truth(const char* cx, const char* cy, const char* scale_digits, i
 // process replay the reference's rand() draws (createRef picks with rand()).
 void mbx_oracle_reset_rand(void) { srand(1); }
 
+// findNucleus on a disk (mp.cpp:1089-1102 after the disk set-up): ball period,
+// Newton (200 iterations), inside-the-disk check. Writes the nucleus as GMP's
+// shortest round-trip digits "d1d2...@exp" and returns the period (0: none).
+int mbx_oracle_nucleus(const char* cx, const char* cy, const char* radius, int maxp, int prec, char* re, char* im, int len) {
+    mpf_t cr, ci, r, nr, ni, dr, di, dist;
+    mpf_init2(cr, prec); mpf_init2(ci, prec); mpf_init2(r, prec); mpf_init2(nr, prec);
+    mpf_init2(ni, prec); mpf_init2(dr, prec); mpf_init2(di, prec); mpf_init2(dist, prec);
+    int result = -1;
+    if (mpf_set_str(cr, cx, 10) == 0 && mpf_set_str(ci, cy, 10) == 0 && mpf_set_str(r, radius, 10) == 0) {
+        result = 0;
+        const int p = g_ballPeriod(cr, ci, r, maxp, prec);
+        mpf_set(nr, cr);
+        mpf_set(ni, ci);
+        if (p > 0 && g_newton(nr, ni, p, prec, 200)) {
+            mpf_sub(dr, nr, cr);
+            mpf_sub(di, ni, ci);
+            mpf_mul(dr, dr, dr);
+            mpf_mul(di, di, di);
+            mpf_add(dist, dr, di);
+            mpf_sqrt(dist, dist);
+            if (mpf_cmp(dist, r) <= 0) result = p;
+        }
+        if (result > 0) {
+            mpf_ptr v[2] = {nr, ni};
+            char* out[2] = {re, im};
+            for (int k = 0; k < 2; ++k) {
+                mp_exp_t e;
+                char* d = mpf_get_str(nullptr, &e, 10, 0, v[k]);
+                snprintf(out[k], (size_t)len, "%s@%ld", d, (long)e);
+                free(d);
+            }
+        }
+    }
+    mpf_clears(cr, ci, r, nr, ni, dr, di, dist, (mpf_ptr)0);
+    return result;
+}
+
 } // extern "C"

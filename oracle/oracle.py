@@ -32,6 +32,8 @@ def load():
         lib.mbx_oracle_bmp.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         lib.mbx_oracle_palette.argtypes = [ctypes.c_void_p]
         lib.mbx_oracle_gamma_value.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib.mbx_oracle_nucleus.restype = ctypes.c_int
+        lib.mbx_oracle_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int]
         _lib = lib
     return _lib
 
@@ -54,6 +56,30 @@ def colorize(values, width, height, ss=1, aux=None, mapping=0, shading=0, densit
     if rc != 0:
         raise ValueError("oracle rejected the colour parameters")
     return out
+
+
+def nucleus(center_re, center_im, radius, max_period, precision_bits):
+    """findNucleus on a disk (ball period + Newton + inside check, serial as
+    mp.cpp:116-223): (period, re, im) with re/im as decimal.Decimal, or None."""
+    from decimal import Decimal, getcontext
+
+    getcontext().prec = max(getcontext().prec, precision_bits // 3 + 50)
+    n = precision_bits + 64
+    a = ctypes.create_string_buffer(n)
+    b = ctypes.create_string_buffer(n)
+    p = load().mbx_oracle_nucleus(center_re.encode(), center_im.encode(), radius.encode(), max_period, precision_bits, a, b, n)
+    if p < 0:
+        raise ValueError("bad nucleus search input")
+    if p == 0:
+        return None
+
+    def dec(s):
+        d, e = s.split("@")
+        neg = d.startswith("-")
+        v = Decimal("0." + d.lstrip("-")).scaleb(int(e))
+        return -v if neg else v
+
+    return p, dec(a.value.decode()), dec(b.value.decode())
 
 
 def gamma_value(l):

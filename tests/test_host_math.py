@@ -57,3 +57,26 @@ def test_floatexp_complex_and_rand_match_libc():
         subprocess.check_call(cmd)
         out = subprocess.run([exe], capture_output=True, text=True)
         assert out.returncode == 0, out.stdout + out.stderr
+
+
+def test_threaded_nucleus_search_matches_serial_oracle():
+    """mbx_find_nucleus runs the period search and the Newton orbit on three
+    threads between 1000 and 1600/2000 bits (ring-buffered recurrences); the
+    nucleus must equal, digit for digit, the serial reference algorithm's
+    (oracle: mp.cpp:116-223), and so must a search whose Newton leaves the disk."""
+    import mbx
+    import oracle
+    import views
+
+    v = views.deep_view(1000)
+    for digits, radius, prec in ((500, "1e-330", 1300), (400, "1e-300", 1200)):
+        cx, cy = v["center_re"][:digits], v["center_im"][:digits]
+        got = mbx.find_nucleus(cx, cy, radius, 100000, prec)
+        want = oracle.nucleus(cx, cy, radius, 100000, prec)
+        if want is None:
+            assert got is None
+            continue
+        from decimal import Decimal
+
+        assert got is not None and got[0] == want[0]
+        assert Decimal(got[1]) == want[1] and Decimal(got[2]) == want[2]
