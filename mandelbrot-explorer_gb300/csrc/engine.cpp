@@ -58,9 +58,9 @@ struct MpfTemp {
 
 // Parallel product rounds (parmul.h): destination k = a[k] * b[k].
 struct MpfMulJob {
-    mpf_ptr r[6];
-    mpf_ptr a[6];
-    mpf_ptr b[6];
+    mpf_ptr r[8];
+    mpf_ptr a[8];
+    mpf_ptr b[8];
 };
 void mpf_mul_job(void* ctx, int k) {
     MpfMulJob* j = static_cast<MpfMulJob*>(ctx);
@@ -925,6 +925,7 @@ int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_
         }
     }
     MpfTemp s1(prec), s2(prec), s3(prec), zr(prec), zi(prec), R(prec), R2m(prec), zabs2(prec), nb(prec), ru(prec), t(prec), tq(prec), F(prec);
+    MpfTemp q1(prec), q2(prec);
     ParSession par(prec >= kParBits4);
     mpf_set_ui(zr, 0);
     mpf_set_ui(zi, 0);
@@ -932,6 +933,59 @@ int ball_period(mpf_srcptr cr, mpf_srcptr ci, mpf_srcptr r, int maxp, mp_bitcnt_
     const double cab = std::hypot(mpf_get_d(cr), mpf_get_d(ci));
     mpf_set_ui(ru, 1);
     mpf_div_2exp(ru, ru, prec > 64 ? prec - 32 : prec / 2);
+    if (prec >= kParBits4 && ParMul::instance().concurrent(7)) {
+        // One round of seven products per step: step p's four with the three
+        // of step p - 1's containment test (|z_{p-1}|^2 and R_{p-1}^2, values
+        // already known), whose verdict is taken before step p's values are
+        // used. Step p's products are then only wasted work when step p - 1
+        // ends the search, except when |z_{p-1}| is too large for the
+        // conversions of step p: that step takes the test on its own first.
+        auto test = [&](int p) -> int { // verdict of step p from q1, q2, R2m: p (period), -1 (escaped), 0 (go on)
+            mpf_add(zabs2, q1, q2);
+            if (mpf_cmp(zabs2, R2m) <= 0) return p;
+            const double zb = std::hypot(mpf_get_d(zr), mpf_get_d(zi));
+            return zb > cab + 2.0 + mpf_get_d(R) ? -1 : 0;
+        };
+        for (int p = 1; p <= maxp; ++p) {
+            if (cancel && (p & 1023) == 0 && cancel->load()) return 0;
+            const double za = std::hypot(mpf_get_d(zr), mpf_get_d(zi));
+            const bool pending = p > 1;
+            bool tested = !pending;
+            if (pending && !(za < 1e150)) {
+                MpfMulJob j = {{q1, q2, R2m}, {zr, zi, R}, {zr, zi, R}};
+                ParMul::instance().run(mpf_mul_job, &j, 3);
+                const int v = test(p - 1);
+                if (v > 0) return v;
+                if (v < 0) return 0;
+                tested = true;
+            }
+            mpf_set_d(t, 2.0 * za);
+            mpf_add(nb, t, R);
+            mpf_set_d(tq, za * za + cab + 1.0);
+            mpf_add(s1, zr, zi);
+            mpf_sub(s2, zr, zi);
+            if (tested) {
+                MpfMulJob j = {{nb, tq, s3, F}, {nb, tq, zr, s1}, {R, ru, zi, s2}};
+                ParMul::instance().run(mpf_mul_job, &j, 4);
+            } else {
+                MpfMulJob j = {{nb, tq, s3, F, q1, q2, R2m}, {nb, tq, zr, s1, zr, zi, R}, {R, ru, zi, s2, zr, zi, R}};
+                ParMul::instance().run(mpf_mul_job, &j, 7);
+                const int v = test(p - 1);
+                if (v > 0) return v;
+                if (v < 0) return 0;
+            }
+            mpf_add(nb, nb, r);
+            mpf_add(nb, nb, tq);
+            mpf_set(R, nb);
+            mpf_add(zr, F, cr);
+            mpf_mul_ui(zi, s3, 2);
+            mpf_add(zi, zi, ci);
+        }
+        MpfMulJob j = {{q1, q2, R2m}, {zr, zi, R}, {zr, zi, R}};
+        ParMul::instance().run(mpf_mul_job, &j, 3);
+        const int v = test(maxp);
+        return v > 0 ? v : 0;
+    }
     for (int p = 1; p <= maxp; ++p) {
         if (cancel && (p & 1023) == 0 && cancel->load()) return 0;
         // the serial step's products in two rounds of independent ones:

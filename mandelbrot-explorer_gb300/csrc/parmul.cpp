@@ -16,7 +16,7 @@ ParMul& ParMul::instance() {
 ParMul::ParMul() {
     pid_ = (long)getpid();
     const unsigned hw = std::thread::hardware_concurrency();
-    const int n = (int)std::min(5u, hw > 1 ? hw - 1 : 0u);
+    const int n = (int)std::min(6u, hw > 1 ? hw - 1 : 0u);
     slots_.reset(new Slot[n > 0 ? n : 1]);
     for (int h = 0; h < n; ++h) helpers_.emplace_back(&ParMul::helper, this, h);
 }

@@ -3,8 +3,8 @@
 // The reference orbit, the ball-arithmetic period search and the Newton
 // nucleus refinement are serial in the iteration index, but each iteration
 // performs several multiplications of the previous iterate's values that do not
-// depend on one another (6 in a Newton step, 4 + 3 in a period-search step, 2
-// in an orbit step). Running them at once on helper threads shortens each
+// depend on one another (6 in a Newton step, 7 in a period-search step when
+// its containment test lags one step, 2 in an orbit step). Up to six helpers. Running them at once on helper threads shortens each
 // iteration; every product is the same GMP (or fixed-point) call on the same
 // operands into a destination of the same precision, so results are bit for
 // bit those of the serial loop. Helpers spin only while a session is open (a

@@ -61,15 +61,17 @@ def test_floatexp_complex_and_rand_match_libc():
 
 def test_threaded_nucleus_search_matches_serial_oracle():
     """mbx_find_nucleus runs the period search and the Newton orbit on three
-    threads between 1000 and 1600/2000 bits (ring-buffered recurrences); the
-    nucleus must equal, digit for digit, the serial reference algorithm's
-    (oracle: mp.cpp:116-223), and so must a search whose Newton leaves the disk."""
+    threads between 1000 and 1600/2000 bits (ring-buffered recurrences), and
+    above as parallel rounds of products (seven per period-search step, its
+    containment test one step behind); the nucleus must equal, digit for digit,
+    the serial reference algorithm's (oracle: mp.cpp:116-223), and so must a
+    search whose Newton leaves the disk."""
     import mbx
     import oracle
     import views
 
     v = views.deep_view(1000)
-    for digits, radius, prec in ((500, "1e-330", 1300), (400, "1e-300", 1200)):
+    for digits, radius, prec in ((500, "1e-330", 1300), (400, "1e-300", 1200), (700, "1e-500", 2200)):
         cx, cy = v["center_re"][:digits], v["center_im"][:digits]
         got = mbx.find_nucleus(cx, cy, radius, 100000, prec)
         want = oracle.nucleus(cx, cy, radius, 100000, prec)
