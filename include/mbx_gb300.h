@@ -15,13 +15,17 @@
 extern "C" {
 #endif
 
-#define MBX_ABI_VERSION 1
+#define MBX_ABI_VERSION 2
 
 /* Coloring flags: same bit values as the reference's ColoringMethod enum
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
 #define MBX_SUPER_SAMPLING 1
 #define MBX_EXTERIOR_DIST_EST 2
 #define MBX_DE_OVERLAY 64
+
+/* What a request renders (ComputeMode, src/engine/compute_backend.h:18). */
+#define MBX_MODE_MANDELBROT 0
+#define MBX_MODE_JULIA 1 /* z0 = the sample, fixed c (Mandel::ComputeJulia, mp.cpp:992-1044) */
 
 /* Arithmetic of the per-sample delta loop. */
 #define MBX_PRECISION_EXACT 0 /* FP64 / FP64-floatexp in the reference's exact operation order */
@@ -61,6 +65,10 @@ typedef struct {
     volatile float* progress;  /* optional: 0..1 progress, written between passes */
     int reuse_reference;       /* 1: reuse the previous frame's reference orbit and BLA table when the view,
                                   size, iteration and coloring parameters are unchanged (zoom-sequence reuse) */
+    int compute_mode;          /* MBX_MODE_*; Julia takes sub 1, coloring 0 or MBX_EXTERIOR_DIST_EST and the
+                                  fixed c below (compute_backend.cpp:268); precision_mode does not apply */
+    const char* fixed_c_re;    /* Julia: fixed c, decimal (ComputeRequest::fixedCRe / fixedCIm) */
+    const char* fixed_c_im;
 } mbx_request;
 
 typedef struct {

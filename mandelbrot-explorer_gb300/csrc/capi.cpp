@@ -39,6 +39,9 @@ int validate(const mbx_request* r, std::string& why) {
     else if (r->row_base < 0 || r->row_base > full_h - r->height) why = "row_base outside the full frame";
     else if (r->sub < 1 || (r->sub % 2) == 0 || r->sub > 255) why = "sub must be odd and in [1, 255]";
     else if (r->max_iterations < 1) why = "max_iterations must be >= 1";
+    else if (r->compute_mode != MBX_MODE_MANDELBROT && r->compute_mode != MBX_MODE_JULIA) why = "unknown compute_mode";
+    else if (r->compute_mode == MBX_MODE_JULIA && (r->sub != 1 || !r->fixed_c_re || !r->fixed_c_im || (r->coloring_method & ~MBX_EXTERIOR_DIST_EST) != 0))
+        why = "Julia takes sub 1, the fixed c and coloring 0 or MBX_EXTERIOR_DIST_EST";
     else if ((r->coloring_method & ~(MBX_SUPER_SAMPLING | MBX_EXTERIOR_DIST_EST | MBX_DE_OVERLAY)) != 0) why = "unsupported coloring_method bits";
     else if (r->precision_mode != MBX_PRECISION_EXACT && r->precision_mode != MBX_PRECISION_MIXED) why = "unknown precision_mode";
     else if (!(r->bailout >= 0.0) || r->bailout > 1e18) why = "bailout must be in [0, 1e18]";
@@ -98,6 +101,10 @@ int mbx_compute_batch(mbx_context* c, const mbx_request* reqs, int n, mbx_stats*
     std::string why;
     for (int i = 0; i < n; ++i) {
         int v = validate(reqs + i, why);
+        if (v == MBX_OK && reqs[i].compute_mode != MBX_MODE_MANDELBROT) {
+            why = "batches hold Mandelbrot frames only";
+            v = MBX_E_INVALID;
+        }
         if (v != MBX_OK) {
             std::lock_guard<std::mutex> l(c->mu);
             c->last_error = "request " + std::to_string(i) + ": " + why;

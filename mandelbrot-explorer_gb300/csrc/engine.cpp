@@ -1868,11 +1868,17 @@ int Engine::compute_frame(const mbx_request& r) {
     out_n_ = out_n;
     cudaError_t e = launch_fill(out_iter, out_norm, out_n, nsamp, st_);
     if (e != cudaSuccess) return fail_cuda("fill", e);
-    hZ_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
-    hzm3_.assign((size_t)MXIT_ + 2, 0.0);
-    hD_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
-    hZfe_.assign((size_t)MXIT_ + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
-    int rc = render(cre, cim, msc, full_h, row_base, r.progress);
+    int rc;
+    if (r.compute_mode == MBX_MODE_JULIA) {
+        reuse_ = false;
+        rc = render_julia(cre, cim, msc, r.fixed_c_re, r.fixed_c_im, full_h, row_base);
+    } else {
+        hZ_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
+        hzm3_.assign((size_t)MXIT_ + 2, 0.0);
+        hD_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
+        hZfe_.assign((size_t)MXIT_ + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
+        rc = render(cre, cim, msc, full_h, row_base, r.progress);
+    }
     if (batch_slot_ && batch_slot_->deferred) return rc; // passes and readback follow in the batch
     if (rc == MBX_OK && !r.outputs_on_device) {
         const double t0 = now_ms();
@@ -2095,6 +2101,70 @@ int Engine::supersample(int ref_it) {
     }
     use_bla_ = saved_bla;
     return rc;
+}
+
+// Julia frames: Mandel::ComputeJulia (mp.cpp:992-1044). The geometry is
+// ComputeJulia's own (its operation order differs from Compute's), then one
+// pass over the grid in double precision.
+int Engine::render_julia(mpf_ptr z_re, mpf_ptr z_im, mpf_ptr scale, const char* fcr, const char* fci, int full_h, int row_base) {
+    method_ = 0;
+    use_floatexp_ = false;
+    ref_period_ = 0;
+    const int rows = full_h > 0 ? full_h : H_;
+    MpfTemp cr, ci;
+    if (mpf_set_str(cr, fcr, 10) != 0 || mpf_set_str(ci, fci, 10) != 0) {
+        err_ = "unparsable fixed c";
+        return MBX_E_INVALID;
+    }
+    mpf_set(scale_, scale);
+    {
+        MpfTemp dw, dh;
+        mpf_set_ui(dw, 2);
+        mpf_div(dw, dw, scale);
+        mpf_set(dh, dw);
+        mpf_mul_ui(dh, dh, rows);
+        mpf_div_ui(dh, dh, W_);
+        mpf_sub(c0_re_, z_re, dw);
+        mpf_sub(c0_im_, z_im, dh);
+        mpf_mul_ui(dx_, dw, 2);
+        mpf_div_ui(dx_, dx_, W_ - 1);
+        mpf_mul_ui(dy_, dh, 2);
+        mpf_div_ui(dy_, dy_, rows - 1);
+        if (row_base != 0) {
+            mpf_mul_ui(dw, dy_, (unsigned long)row_base);
+            mpf_add(c0_im_, c0_im_, dw);
+        }
+    }
+    JuliaParams p;
+    p.g = geom();
+    p.z0r = mpf_ld(c0_re_);
+    p.z0i = mpf_ld(c0_im_);
+    p.dx = mpf_ld(dx_);
+    p.dy = mpf_ld(dy_);
+    p.cr = mpf_ld(cr);
+    p.ci = mpf_ld(ci);
+    const int n = W_ * H_;
+    cudaMemsetAsync(dctr_, 0, sizeof(Counters), st_);
+    DeviceFrame f = frame_view();
+    const double t0 = now_ms();
+    cudaEventRecord(ev0_, st_);
+    cudaError_t e = launch_julia(f, p, std::min((n + 127) / 128, nsm_ * 8), 128, st_);
+    cudaEventRecord(ev1_, st_);
+    ++stats_.kernel_launches;
+    ++stats_.passes;
+    if (e != cudaSuccess) return fail_cuda("julia launch", e);
+    cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    e = cudaStreamSynchronize(st_);
+    stats_.kernel_ms += now_ms() - t0;
+    if (e != cudaSuccess) return fail_cuda("julia pass", e);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    stats_.pass_gpu_ms += ms;
+    stats_.steps += (long long)hctr_->steps;
+    stats_.effective_iterations += (long long)hctr_->effective_iters;
+    stats_.interior += (int)hctr_->interior;
+    stats_.samples += n;
+    return MBX_OK;
 }
 
 // Shallow frames (scale <= 1e6, mp.cpp:1444-1519) and their SS sub-samples.

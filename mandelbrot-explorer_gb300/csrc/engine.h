@@ -102,6 +102,7 @@ class Engine {
     int compute_frame(const mbx_request& r);
     int render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int row_base, volatile float* progress);
     int render_shallow(volatile float* progress);
+    int render_julia(mpf_ptr z_re, mpf_ptr z_im, mpf_ptr scale, const char* fcr, const char* fci, int full_h, int row_base);
     int shallow_samples(const std::vector<uint64_t>& samples);
     int glitch_loop(std::vector<uint64_t>& pending, int& ref_it, bool have, int* nr, volatile float* progress);
     int supersample(int ref_it);

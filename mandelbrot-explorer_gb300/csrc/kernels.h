@@ -164,6 +164,13 @@ struct ShallowParams {
     int simd_semantics;      // 1: lane-refill kernel (float result), 0: floatPointCompute
 };
 
+// Julia frames (Mandel::ComputeJulia, mp.cpp:992-1044): z0 = c0 + (dx j, dy i).
+struct JuliaParams {
+    FrameGeom g;
+    double z0r, z0i, dx, dy; // lower-left sample and spacings (mpf_get_ld)
+    double cr, ci;           // the fixed c
+};
+
 struct DeviceFrame {
     OrbitView orbit;
     BlaView bla;
@@ -179,6 +186,7 @@ cudaError_t launch_fill(float* iter, float* normal, int32_t* escN, size_t n, cud
 cudaError_t launch_fp64_pass(const DeviceFrame& f, const Fp64Params& p, int blocks, int threads, cudaStream_t st);
 cudaError_t launch_fe_pass(const DeviceFrame& f, const FeParams& p, int blocks, int threads, cudaStream_t st);
 cudaError_t launch_shallow(const DeviceFrame& f, const ShallowParams& p, int blocks, int threads, cudaStream_t st);
+cudaError_t launch_julia(const DeviceFrame& f, const JuliaParams& p, int blocks, int threads, cudaStream_t st);
 cudaError_t launch_bla_build(const double2* Z, const double2* D, int reflen, double eps, double dcmax, bool ede,
                              double* r2, double4* ab, double4* ce, const int* off, const int* size, int nlev,
                              unsigned long long* rmax2_bits, cudaStream_t st);

@@ -932,6 +932,76 @@ __device__ float shallow_lane(double cr, double ci, int mxit, const FrameGeom& g
     }
 }
 
+// One Julia sample with the per-lane arithmetic of solveJuliaShallowSimdList
+// (mp.cpp:534-636): z0 the sample, c fixed, D_0 = 1 and D' = 2 z D under EDE.
+// nout: escape index (0 when z0 is already outside), -1 interior.
+__device__ float julia_lane(double zr, double zi, double cr, double ci, int mxit, const FrameGeom& g, int* nout) {
+    double zrad = (zr * zr) + (zi * zi);
+    *nout = -1;
+    if (zrad > g.ESC2) {
+        *nout = 0;
+        return g.ede ? (float)(sqrt(zrad) * log(zrad)) : (float)(-log(log(zrad) / 2 / kLn2) / kLn2);
+    }
+    double dr = 1.0, di = 0.0, jv = 0.0;
+    for (;;) {
+        double ndr = dr, ndi = di;
+        if (g.ede) {
+            ndr = 2.0 * ((dr * zr) - (di * zi));
+            ndi = 2.0 * ((dr * zi) + (di * zr));
+        }
+        const double nzr = ((zr * zr) - (zi * zi)) + cr;
+        const double nzi = (2.0 * (zr * zi)) + ci;
+        zr = nzr;
+        zi = nzi;
+        dr = ndr;
+        di = ndi;
+        zrad = (zr * zr) + (zi * zi);
+        const double jnext = jv + 1.0;
+        if (zrad > g.ESC2) {
+            *nout = (int)jv + 1;
+            if (g.ede) {
+                const double denom = sqrt((dr * dr) + (di * di));
+                return denom > 0.0 ? (float)(sqrt(zrad) * log(zrad) / denom) : 0.0f;
+            }
+            return (float)(jv + 1 - log(log(zrad) / 2 / kLn2) / kLn2);
+        }
+        if (jnext >= (double)mxit) return -2.0f;
+        jv = jnext;
+    }
+}
+
+// ComputeJulia's frame (mp.cpp:1019-1041): every sample of the grid, the EDE
+// value divided by (float)dx.
+__global__ void __launch_bounds__(128) k_julia(DeviceFrame f, JuliaParams p) {
+    const FrameGeom& g = p.g;
+    unsigned long long n_eff = 0, n_steps = 0;
+    unsigned int n_int = 0;
+    const int n = g.W * g.H;
+    for (;;) {
+        if (cancelled(f)) break;
+        const int s = (int)atomicAdd(&f.ctr->next, 1u);
+        if (s >= n) break;
+        const int i = s / g.W, j = s - i * g.W;
+        const double imag = p.z0i + p.dy * i;
+        int nout = -1;
+        float v = julia_lane(p.z0r + p.dx * j, imag, p.cr, p.ci, g.mxit, g, &nout);
+        if (g.ede && v >= 0.0f) v /= (float)p.dx;
+        f.out.iter[s] = v;
+        if (f.out.escN) f.out.escN[s] = nout;
+        if (nout >= 0) {
+            n_eff += (unsigned long long)nout;
+            n_steps += (unsigned long long)nout;
+        } else {
+            n_eff += (unsigned long long)g.mxit;
+            n_steps += (unsigned long long)g.mxit;
+            ++n_int;
+        }
+    }
+    atomicAdd(&f.ctr->effective_iters, n_eff);
+    atomicAdd(&f.ctr->steps, n_steps);
+    atomicAdd(&f.ctr->interior, n_int);
+}
+
 // Base pass (mp.cpp:1483-1519) in grid mode, or adaptive-SS sub-samples
 // (mp.cpp:1920-1969) from a key list.
 __global__ void __launch_bounds__(128) k_shallow(DeviceFrame f, ShallowParams p) {
@@ -1096,6 +1166,11 @@ cudaError_t launch_fe_pass(const DeviceFrame& f, const FeParams& p, int blocks, 
     k_fe_pass<<<blocks, threads, 0, st>>>(f, p);
     return cudaGetLastError();
 }
+cudaError_t launch_julia(const DeviceFrame& f, const JuliaParams& p, int blocks, int threads, cudaStream_t st) {
+    k_julia<<<blocks, threads, 0, st>>>(f, p);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_shallow(const DeviceFrame& f, const ShallowParams& p, int blocks, int threads, cudaStream_t st) {
     k_shallow<<<blocks, threads, 0, st>>>(f, p);
     return cudaGetLastError();

@@ -32,6 +32,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libmbx_gb300.so")
 SUPER_SAMPLING = 1
 EXTERIOR_DIST_EST = 2
 DE_OVERLAY = 64
+MODE_MANDELBROT, MODE_JULIA = 0, 1
 EMPTYPIXEL = -10.0
 
 PRECISION_EXACT = 0
@@ -61,6 +62,9 @@ class _Request(ctypes.Structure):
         ("escape_iteration", ctypes.c_void_p),
         ("progress", ctypes.c_void_p),
         ("reuse_reference", ctypes.c_int),
+        ("compute_mode", ctypes.c_int),
+        ("fixed_c_re", ctypes.c_char_p),
+        ("fixed_c_im", ctypes.c_char_p),
     ]
 
 
@@ -282,6 +286,9 @@ class ComputeRequest:
     want_escape_iteration: bool = True
     progress: Optional[ctypes.c_float] = None
     reuse_reference: bool = False
+    compute_mode: int = 0  # MODE_MANDELBROT / MODE_JULIA (ComputeMode)
+    fixed_c_re: Optional[str] = None  # Julia: the fixed c
+    fixed_c_im: Optional[str] = None
 
     def sample_count(self) -> int:
         return self.width * self.height * self.sub * self.sub
@@ -394,6 +401,9 @@ class CudaComputeBackend:
             en,
             ctypes.cast(ctypes.pointer(req.progress), ctypes.c_void_p) if req.progress is not None else None,
             1 if req.reuse_reference else 0,
+            req.compute_mode,
+            req.fixed_c_re.encode() if req.fixed_c_re is not None else None,
+            req.fixed_c_im.encode() if req.fixed_c_im is not None else None,
         )
         return r, (req.iterations, req.normal, req.escape_iteration)
 

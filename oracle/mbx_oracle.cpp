@@ -2321,6 +2321,98 @@ int mbx_oracle_truth(const char* cx, const char* cy, const char* scale_digits, i
 // process replay the reference's rand() draws (createRef picks with rand()).
 void mbx_oracle_reset_rand(void) { srand(1); }
 
+// Mandel::ComputeJulia (mp.cpp:992-1044): geometry in mpf as written there,
+// then per sample the scalar semantics of solveJuliaShallowSimdList
+// (mp.cpp:534-636): z0 the sample, c fixed, D_0 = 1 and D' = 2 z D under EDE.
+// escn receives the escape index (jv + 1; 0 when z0 is already outside; -1
+// interior), which the reference does not output.
+int mbx_oracle_julia(const char* cx, const char* cy, const char* scale_digits, int prec_bits, const char* fcr, const char* fci, int W, int H,
+                     int mxit, int cmethod, double bailout, int full_h, int row_base, float* iter, int32_t* escn) {
+    if (W < 2 || H < 1 || mxit < 1 || (cmethod & ~CM_EDE) != 0) return -1;
+    if (full_h <= 0) full_h = H;
+    if (full_h < H || row_base < 0 || row_base > full_h - H) return -1;
+    mpf_set_default_prec((mp_bitcnt_t)prec_bits);
+    mpf_t z0r, z0i, sc, cr, ci, dw, dh, c0r, c0i, dx, dy;
+    mpf_init2(z0r, prec_bits); mpf_init2(z0i, prec_bits); mpf_init2(sc, prec_bits); mpf_init2(cr, prec_bits); mpf_init2(ci, prec_bits);
+    mpf_init2(c0r, prec_bits); mpf_init2(c0i, prec_bits); mpf_init2(dx, prec_bits); mpf_init2(dy, prec_bits);
+    int rc = 0;
+    if (mpf_set_str(z0r, cx, 10) || mpf_set_str(z0i, cy, 10) || mpf_set_str(sc, scale_digits, 10) || mpf_set_str(cr, fcr, 10) || mpf_set_str(ci, fci, 10)) rc = -1;
+    if (rc == 0) {
+        mpf_init_set_ui(dw, 2);
+        mpf_div(dw, dw, sc);
+        mpf_init_set(dh, dw);
+        mpf_mul_ui(dh, dh, full_h);
+        mpf_div_ui(dh, dh, W);
+        mpf_sub(c0r, z0r, dw);
+        mpf_sub(c0i, z0i, dh);
+        mpf_mul_ui(dx, dw, 2);
+        mpf_div_ui(dx, dx, W - 1);
+        mpf_mul_ui(dy, dh, 2);
+        mpf_div_ui(dy, dy, full_h - 1);
+        if (row_base != 0) {
+            mpf_mul_ui(dw, dy, (unsigned long)row_base);
+            mpf_add(c0i, c0i, dw);
+        }
+        mpf_clear(dw);
+        mpf_clear(dh);
+        const float escf = (float)(bailout > 0 ? bailout : 1e8);
+        const double ESC2 = (double)(escf * escf); // escapeRadiusSquared (mp.h:115-118)
+        const double LG2 = std::log(2.0);
+        const double cRe = mpf_ld(cr), cIm = mpf_ld(ci);
+        const double z0Re = mpf_ld(c0r), z0Im = mpf_ld(c0i);
+        const double ddx = mpf_ld(dx), ddy = mpf_ld(dy);
+        const bool ede = (cmethod & CM_EDE) != 0;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int i = 0; i < H; ++i) {
+            const double imag = z0Im + ddy * i;
+            for (int j = 0; j < W; ++j) {
+                double zr = z0Re + ddx * j, zi = imag;
+                double zrad = zr * zr + zi * zi;
+                float result = -2.0f;
+                int n = -1;
+                if (zrad > ESC2) {
+                    result = ede ? (float)(std::sqrt(zrad) * std::log(zrad)) : (float)(-std::log(std::log(zrad) / 2 / LG2) / LG2);
+                    n = 0;
+                } else {
+                    double dr = 1.0, di = 0.0, jv = 0.0;
+                    for (;;) {
+                        double ndr = dr, ndi = di;
+                        if (ede) {
+                            ndr = 2.0 * (dr * zr - di * zi);
+                            ndi = 2.0 * (dr * zi + di * zr);
+                        }
+                        const double nzr = zr * zr - zi * zi + cRe;
+                        const double nzi = 2.0 * (zr * zi) + cIm;
+                        zr = nzr;
+                        zi = nzi;
+                        dr = ndr;
+                        di = ndi;
+                        zrad = zr * zr + zi * zi;
+                        const double jnext = jv + 1.0;
+                        if (zrad > ESC2) {
+                            if (ede) {
+                                const double denom = std::sqrt(dr * dr + di * di);
+                                result = denom > 0.0 ? (float)(std::sqrt(zrad) * std::log(zrad) / denom) : 0.0f;
+                            } else {
+                                result = (float)(jv + 1 - std::log(std::log(zrad) / 2 / LG2) / LG2);
+                            }
+                            n = (int)jv + 1;
+                            break;
+                        }
+                        if (jnext >= (double)mxit) break;
+                        jv = jnext;
+                    }
+                }
+                if (ede && result >= 0.0f) result /= (float)ddx;
+                iter[(size_t)i * W + j] = result;
+                if (escn) escn[(size_t)i * W + j] = n;
+            }
+        }
+    }
+    mpf_clears(z0r, z0i, sc, cr, ci, c0r, c0i, dx, dy, (mpf_ptr)0);
+    return rc;
+}
+
 // findNucleus on a disk (mp.cpp:1089-1102 after the disk set-up): ball period,
 // Newton (200 iterations), inside-the-disk check. Writes the nucleus as GMP's
 // shortest round-trip digits "d1d2...@exp" and returns the period (0: none).

@@ -32,6 +32,8 @@ def load():
         lib.mbx_oracle_bmp.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         lib.mbx_oracle_palette.argtypes = [ctypes.c_void_p]
         lib.mbx_oracle_gamma_value.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib.mbx_oracle_julia.restype = ctypes.c_int
+        lib.mbx_oracle_julia.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] + [ctypes.c_char_p] * 2 + [ctypes.c_int] * 4 + [ctypes.c_double] + [ctypes.c_int] * 2 + [ctypes.c_void_p] * 2
         lib.mbx_oracle_nucleus.restype = ctypes.c_int
         lib.mbx_oracle_nucleus.argtypes = [ctypes.c_char_p] * 3 + [ctypes.c_int] * 2 + [ctypes.c_char_p] * 2 + [ctypes.c_int]
         _lib = lib
@@ -56,6 +58,17 @@ def colorize(values, width, height, ss=1, aux=None, mapping=0, shading=0, densit
     if rc != 0:
         raise ValueError("oracle rejected the colour parameters")
     return out
+
+
+def julia(center_re, center_im, scale, fixed_c_re, fixed_c_im, width, height, max_iterations, coloring_method=0, bailout=1e8, full_height=0, row_base=0, precision_bits=0):
+    """Mandel::ComputeJulia restated: (iterations float32, escape index int32)."""
+    it = np.empty(width * height, np.float32)
+    en = np.empty(width * height, np.int32)
+    prec = precision_bits or precision_for_scale(scale)
+    rc = load().mbx_oracle_julia(center_re.encode(), center_im.encode(), scale.encode(), prec, fixed_c_re.encode(), fixed_c_im.encode(), width, height, max_iterations, coloring_method, float(bailout), full_height, row_base, it.ctypes.data, en.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle rejected the Julia request")
+    return it, en
 
 
 def nucleus(center_re, center_im, radius, max_period, precision_bits):

@@ -5,7 +5,8 @@
 // (plus the DE-overlay buffer when requested) for parity fixtures.
 //
 // usage: mbx_refdump <cx> <cy> <scale-digits> <W> <H> <mxit> <sub> <cmethod>
-//                    <out.f32> [full_h row_base] [--time trials]
+//                    <out.f32> [full_h row_base] [--time trials] [--julia <cre> <cim>]
+// With --julia the frame is Mandel::ComputeJulia for the fixed c (cre, cim).
 // Precision rule of src/tools/verify.cpp:runCase: bits = digits*log2(10)+64.
 #include <gmp.h>
 #include <chrono>
@@ -31,12 +32,21 @@ int main(int argc, char** argv) {
     const char* out = argv[9];
     int full_h = 0, row_base = 0, trials = 0;
     int a = 10;
-    if (argc > 11 && strcmp(argv[10], "--time") != 0) {
+    if (argc > 11 && strncmp(argv[10], "--", 2) != 0) {
         full_h = atoi(argv[10]);
         row_base = atoi(argv[11]);
         a = 12;
     }
-    if (argc > a + 1 && strcmp(argv[a], "--time") == 0) trials = atoi(argv[a + 1]);
+    if (argc > a + 1 && strcmp(argv[a], "--time") == 0) {
+        trials = atoi(argv[a + 1]);
+        a += 2;
+    }
+    const char* jre = nullptr;
+    const char* jim = nullptr;
+    if (argc > a + 2 && strcmp(argv[a], "--julia") == 0) {
+        jre = argv[a + 1];
+        jim = argv[a + 2];
+    }
     int precision = (int)(scale.size() * log(10) / log(2)) + 64;
     if (const char* e = getenv("MANDEL_PREC")) precision = (int)(atol(e) * 3.3219281 + 64.0);
     mpf_set_default_prec(precision);
@@ -55,7 +65,16 @@ int main(int argc, char** argv) {
         m.setPrecision(precision);
         if (cmethod & (ColoringMethod::DE_OVERLAY | ColoringMethod::NORMAL_MAP)) m.setNormalBuffer(normal.data());
         auto t0 = std::chrono::steady_clock::now();
-        m.Compute(mcx, mcy, msc, mxit, cmethod, full_h, row_base);
+        if (jre) {
+            mpf_t fr, fi;
+            mpf_init_set_str(fr, jre, 10);
+            mpf_init_set_str(fi, jim, 10);
+            m.ComputeJulia(mcx, mcy, msc, fr, fi, mxit, cmethod, full_h, row_base);
+            mpf_clear(fr);
+            mpf_clear(fi);
+        } else {
+            m.Compute(mcx, mcy, msc, mxit, cmethod, full_h, row_base);
+        }
         double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (s < best) best = s;
     }

@@ -59,3 +59,13 @@ def bmp_rgb(bmp, width, height):
 
 def color_kwargs(case):
     return {k: case[k] for k in ("mapping", "shading", "density", "light_az", "light_el", "relief_strength", "de_k")}
+
+
+def load_julia_cases():
+    with open(os.path.join(GOLDEN, "julia_cases.json")) as f:
+        return json.load(f)
+
+
+def load_julia_fixture(name):
+    """The reference engine's Mandel::ComputeJulia output for a case (float32)."""
+    return np.fromfile(os.path.join(GOLDEN, "ref_julia_%s.f32" % name), dtype="<f4")

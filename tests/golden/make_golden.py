@@ -6,6 +6,8 @@
   of cases.json with MANDEL_COARSE=0 and MANDEL_BAILOUT set to the case's
   bailout. Raw little-endian float32, the reference's buffer layout, followed
   by the DE-overlay buffer when the case sets DE_OVERLAY.
+* ``ref_julia_<case>.f32`` — the same engine's Mandel::ComputeJulia for each
+  case of julia_cases.json (the dump tool's --julia option).
 * ``truth_<name>.f32`` — byte copies of the reference's own golden files
   (tests/golden/*.f32 there: arbitrary-precision ground truth, not engine
   output) for the cases its verify harness checks against them.
@@ -43,6 +45,16 @@ def main():
         env = dict(os.environ, MANDEL_BAILOUT=repr(float(c["bailout"])), MANDEL_COARSE="0", OMP_NUM_THREADS=str(os.cpu_count()))
         out = os.path.join(HERE, "ref_%s.f32" % name)
         cmd = [DUMP, c["center_re"], c["center_im"], c["scale"], str(c["width"]), str(c["height"]), str(c["max_iterations"]), str(c["sub"]), str(c["coloring_method"]), out]
+        subprocess.check_call(cmd, env=env, stdout=subprocess.DEVNULL)
+        print("wrote", out)
+    jcases = json.load(open(os.path.join(HERE, "julia_cases.json")))
+    for name, c in jcases.items():
+        env = dict(os.environ, MANDEL_BAILOUT=repr(float(c["bailout"])), OMP_NUM_THREADS=str(os.cpu_count()))
+        out = os.path.join(HERE, "ref_julia_%s.f32" % name)
+        cmd = [DUMP, c["center_re"], c["center_im"], c["scale"], str(c["width"]), str(c["height"]), str(c["max_iterations"]), "1", str(c["coloring_method"]), out]
+        if c.get("full_height"):
+            cmd += [str(c["full_height"]), str(c["row_base"])]
+        cmd += ["--julia", c["fixed_c_re"], c["fixed_c_im"]]
         subprocess.check_call(cmd, env=env, stdout=subprocess.DEVNULL)
         print("wrote", out)
     for name, fn in TRUTH.items():

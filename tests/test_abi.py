@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = mbx.load_library()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.mbx_abi_version() == 1
+    assert lib.mbx_abi_version() == 2
 
 
 def test_no_cpu_fallback_without_device():
@@ -38,3 +38,18 @@ def test_no_cpu_fallback_without_device():
 def test_unknown_backend_name_rejected():
     with pytest.raises(ValueError):
         mbx.create_compute_backend("d3d11")
+
+
+def test_request_layout_matches_header(tmp_path):
+    """The binding's mbx_request mirror has the header's size and field offsets."""
+    src = tmp_path / "layout.c"
+    fields = [f for f, _ in mbx._Request._fields_]
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "mbx_gb300.h"\nint main(void){printf("%zu", sizeof(mbx_request));'
+                   + "".join('printf(" %%zu", offsetof(mbx_request, %s));' % f for f in fields) + "return 0;}\n")
+    exe = tmp_path / "layout"
+    import subprocess
+
+    subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    vals = [int(x) for x in subprocess.check_output([str(exe)], text=True).split()]
+    assert vals[0] == ctypes.sizeof(mbx._Request)
+    assert vals[1:] == [getattr(mbx._Request, f).offset for f in fields]

@@ -75,3 +75,21 @@ def test_oracle_meets_reference_truth(name):
     if "mean" in tol:
         assert d.mean() <= tol["mean"]
         assert np.sort(d)[int(np.ceil(0.99 * d.size)) - 1] <= tol["p99"]
+
+
+JULIA = __import__("conftest").load_julia_cases()
+
+
+@pytest.mark.parametrize("name", sorted(JULIA))
+def test_oracle_julia_matches_reference_build(name):
+    from conftest import load_julia_fixture
+
+    c = JULIA[name]
+    it, en = oracle.julia(c["center_re"], c["center_im"], c["scale"], c["fixed_c_re"], c["fixed_c_im"], c["width"], c["height"], c["max_iterations"], c["coloring_method"], c["bailout"], c.get("full_height", 0), c.get("row_base", 0))
+    ref = load_julia_fixture(name)
+    assert np.array_equal(ref < -1.5, it < -1.5)
+    assert np.array_equal(en < 0, it < -1.5)
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert np.array_equal(ref.view(np.uint32), it.view(np.uint32)), "oracle differs from the reference build"
+    else:
+        np.testing.assert_allclose(it, ref, rtol=1e-6, atol=0)
