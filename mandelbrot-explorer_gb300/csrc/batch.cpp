@@ -331,7 +331,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             return MBX_E_CANCELLED;
         }
         bs.pass_gpu_ms = ms;
-        bs.kernel_launches = 7;
+        bs.kernel_launches = 9; // per phase FP32, double-float (two widths), FP64; and the gate
         bs.passes = 2;
         for (int c = 0; c < 6; ++c) {
             const Counters& k = h_ctr_[c];

@@ -1445,7 +1445,7 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         return r;
     };
     e = run_df_pass(queue_frame(drerun_keys_.p, 0, drerun2_keys_.p, 1));
-    ++stats_.kernel_launches;
+    stats_.kernel_launches += 2; // narrow and wide variants, one of which runs
     if (e != cudaSuccess) return fail_cuda("double-float rerun launch", e);
     cudaEventRecord(evd_, st_);
     e = run_rerun_pass(queue_frame(drerun2_keys_.p, 1, nullptr, 2));

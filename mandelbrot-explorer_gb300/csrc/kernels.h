@@ -207,6 +207,9 @@ struct MixedParams {
     int orbit_in_smem;       // stage the whole (periodic) orbit into shared memory
     int smem_entries;
     float wmax2, wmin2;      // |w|^2 rescale window
+    unsigned wide_from = 0;  // rerun passes launched in two widths: the 32-lane
+                             // variant runs when the queue holds >= wide_from
+                             // entries, the narrow one below (0: no selection)
 };
 // The lane passes are launched by Engine::run_mixed_pass / run_df_pass /
 // run_rerun_pass (kernels_mixed.cu), which own their per-reference tables.
@@ -243,7 +246,14 @@ struct BatchArgs {
     uint64_t* next_queue;    // where samples this pass cannot vouch for go (null: none)
     unsigned* view_interior; // probe pass: interior count per view (null otherwise)
     volatile int* cancel;
+    unsigned wide_from = 0;  // as MixedParams::wide_from
 };
+// Rerun queues at least this many entries per SM take 32 lanes per warp
+// (fewer warp instructions for the same samples); shorter ones 8 (less
+// divergence on each sample's latency chain). Measured on the 1e-300 frame's
+// double-float queue: 19,932 entries 4.23 -> 2.89 ms wide, 4,965 entries 1.88
+// (narrow) vs 2.76 ms (wide).
+constexpr unsigned kWideLanesPerSm = 96;
 constexpr int kBatchViewShift = 56;
 constexpr int kBatchMaxViews = 256;
 cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st); // tier 0 FP32, 1 double-float, 2 FP64

@@ -82,6 +82,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     const FrameGeom& g = p.g;
     const V2* orb = orbit;
     const int n = f.px.n_dev ? min((int)*f.px.n_dev, f.px.n) : f.px.n;
+    // Of a two-width launch only the variant chosen by the queue length runs.
+    if (p.wide_from && ((unsigned)n >= p.wide_from) != (LANES == 32)) return;
     // Blocks past the work leave at once (the work counter hands all n entries
     // to the lower blocks), before any orbit staging.
     if ((long long)blockIdx.x * (MAXT / 32) * LANES >= n) return;
@@ -206,6 +208,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     for (int v = threadIdx.x; v < nv; v += MAXT) s_base[v] = a.views[v].base;
     __syncthreads();
     const unsigned n = a.queue ? min(*a.queue_n, a.capacity) : a.total;
+    if (a.wide_from && (n >= a.wide_from) != (LANES == 32)) return;
     if ((unsigned long long)blockIdx.x * (MAXT / 32) * LANES >= n) return;
     const unsigned take = LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u);
     const unsigned lane_id = threadIdx.x & 31;
@@ -433,12 +436,18 @@ cudaError_t Engine::run_df_pass(const DeviceFrame& f) {
     if (!(bla_.use && dbladf_.p)) g.bla.use = 0;
     const int threads = 128;
     const int blocks = std::max(1, std::min((f.px.n + 31) / 32, nsm_ * 4));
-    auto kern = k_lane_pass<df32, 128, 2, 8>;
+    // the queue length is known only on the device: both widths are launched
+    // and the one it selects runs
+    p.wide_from = kWideLanesPerSm * (unsigned)nsm_;
+    auto narrow = k_lane_pass<df32, 128, 2, 8>;
+    auto wide = k_lane_pass<df32, 128, 2, 32>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(narrow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    kern<<<blocks, threads, smem, st_>>>(g, p, dbladf_.p, dZdf_.p);
+    narrow<<<blocks, threads, smem, st_>>>(g, p, dbladf_.p, dZdf_.p);
+    wide<<<std::max(1, std::min((f.px.n + 127) / 128, nsm_ * 4)), threads, smem, st_>>>(g, p, dbladf_.p, dZdf_.p);
     return cudaGetLastError();
 }
 
@@ -458,7 +467,10 @@ cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_
     if (tier == 0) {
         k_batch_pass<float, 256, 2><<<nsm * 2, 256, 0, st>>>(a);
     } else if (tier == 1) {
-        k_batch_pass<df32, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(a);
+        BatchArgs b = a;
+        b.wide_from = kWideLanesPerSm * (unsigned)nsm;
+        k_batch_pass<df32, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(b);
+        k_batch_pass<df32, 128, 2, 32><<<nsm * 4, 128, 0, st>>>(b);
     } else {
         k_batch_pass<double, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(a);
     }
