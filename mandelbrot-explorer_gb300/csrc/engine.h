@@ -220,6 +220,11 @@ class Engine {
     DevBuf<df2> dZdf_;
     DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample lane cost
     DevBuf<float2> dpgrid_;   // and the probe pass's cost per 8x8 cell
+    DevBuf<double> ddpxy_;    // mixed passes: sample offsets per column then per row
+    DevBuf<float> ddpxyf_;    // (their float roundings)
+    std::vector<double> hdpxy_;
+    std::vector<float> hdpxyf_;
+    int dpxy_w_ = 0;
     DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
     DevBuf<uint64_t> drerun2_keys_;           // double-float pass: queue for the FP64 pass
     DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position

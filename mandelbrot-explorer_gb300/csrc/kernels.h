@@ -207,6 +207,15 @@ struct MixedParams {
     int orbit_in_smem;       // stage the whole (periodic) orbit into shared memory
     int smem_entries;
     float wmax2, wmin2;      // |w|^2 rescale window
+    // Per supersampled column / row: the sample's offset from the reference in
+    // pixels, arr[1] + arr[3] / sub - ref_x (and the same for rows), computed
+    // on the host with the lane's own double expression, plus its float
+    // rounding: the per-sample setup then needs no FP64 arithmetic. Null:
+    // computed in the lane.
+    const double* dpx_tab = nullptr;
+    const double* dpy_tab = nullptr;
+    const float* dpx_tabf = nullptr;
+    const float* dpy_tabf = nullptr;
     unsigned wide_from = 0;  // rerun passes launched in two widths: the 32-lane
                              // variant runs when the queue holds >= wide_from
                              // entries, the narrow one below (0: no selection)

@@ -367,6 +367,26 @@ int Engine::measure_fma_peak(int fp64, double* tflops) {
 
 int Engine::prepare_mixed() {
     const int len = orbit_len_;
+    {
+        // sample offsets from the reference per supersampled column and row
+        // (the lane's expression, evaluated here once per frame)
+        const int nx = W_ * SUB_, ny = H_ * SUB_;
+        hdpxy_.resize((size_t)(nx + ny));
+        hdpxyf_.resize((size_t)(nx + ny));
+        for (int k = 0; k < nx; ++k) {
+            const int a1 = k / SUB_, a3 = k % SUB_ - SUB_ / 2;
+            hdpxy_[(size_t)k] = a1 + (double)a3 / SUB_ - ref_x_;
+        }
+        for (int k = 0; k < ny; ++k) {
+            const int a0 = k / SUB_, a2 = k % SUB_ - SUB_ / 2;
+            hdpxy_[(size_t)(nx + k)] = a0 + (double)a2 / SUB_ - ref_y_;
+        }
+        for (size_t k = 0; k < hdpxy_.size(); ++k) hdpxyf_[k] = (float)hdpxy_[k];
+        if (!ensure(ddpxy_, hdpxy_.size()) || !ensure(ddpxyf_, hdpxyf_.size())) return MBX_E_NOMEM;
+        cudaMemcpyAsync(ddpxy_.p, hdpxy_.data(), sizeof(double) * hdpxy_.size(), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(ddpxyf_.p, hdpxyf_.data(), sizeof(float) * hdpxyf_.size(), cudaMemcpyHostToDevice, st_);
+        dpxy_w_ = nx;
+    }
     if (!ensure(dZf_, (size_t)len + 4) || !ensure(dZdf_, (size_t)len + 4)) return MBX_E_NOMEM;
     k_orbit_to_float<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZf_.p, len);
     k_orbit_to_df<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZdf_.p, len);
@@ -400,6 +420,12 @@ MixedParams Engine::mixed_params() const {
     p.smem_entries = orbit_len_;
     p.wmax2 = mixed_wmax2_;
     p.wmin2 = 1.0f / mixed_wmax2_;
+    if (ddpxy_.p && dpxy_w_ == W_ * SUB_) {
+        p.dpx_tab = ddpxy_.p;
+        p.dpy_tab = ddpxy_.p + dpxy_w_;
+        p.dpx_tabf = ddpxyf_.p;
+        p.dpy_tabf = ddpxyf_.p + dpxy_w_;
+    }
     return p;
 }
 

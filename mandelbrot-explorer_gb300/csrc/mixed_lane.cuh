@@ -408,16 +408,34 @@ MBX_HD FE lane_dc_re(const MixedParams& p, const Lane<T>& L) { return fe_mul_d(p
 template <class T>
 MBX_HD FE lane_dc_im(const MixedParams& p, const Lane<T>& L) { return fe_mul_d(p.dyfe, L.dpy); }
 
+// A sample offset in the lane type: the float table's entry for FP32 lanes
+// (no FP64 conversion), else the double value converted.
+template <class T>
+MBX_HD T lane_offset(const float* tabf, int k, double d) { return (T)d; }
+template <>
+MBX_HD float lane_offset<float>(const float* tabf, int k, double d) { return tabf ? tabf[k] : (float)d; }
+
 // Start sample arr = {row, col, subrow, subcol} as pass entry i.
 template <class T>
 MBX_HDF void lane_setup_at(Lane<T>& L, int i, const int* arr, const MixedParams& p, const TE<T> dxf, const TE<T> dyf, const typename LaneReal<T>::V2* orb) {
     const FrameGeom& g = p.g;
     L.i = i;
-    L.oidx = (arr[0] * g.sub + g.sub / 2 + arr[2]) * g.W * g.sub + (arr[1] * g.sub + g.sub / 2 + arr[3]);
-    L.dpx = arr[1] + (double)arr[3] / g.sub - p.ref_x;
-    L.dpy = arr[0] + (double)arr[2] / g.sub - p.ref_y;
+    const int cy = arr[0] * g.sub + g.sub / 2 + arr[2], cx = arr[1] * g.sub + g.sub / 2 + arr[3];
+    L.oidx = cy * g.W * g.sub + cx;
+    T ox, oy;
+    if (p.dpx_tab) {
+        L.dpx = p.dpx_tab[cx];
+        L.dpy = p.dpy_tab[cy];
+        ox = lane_offset<T>(p.dpx_tabf, cx, L.dpx);
+        oy = lane_offset<T>(p.dpy_tabf, cy, L.dpy);
+    } else {
+        L.dpx = arr[1] + (double)arr[3] / g.sub - p.ref_x;
+        L.dpy = arr[0] + (double)arr[2] / g.sub - p.ref_y;
+        ox = (T)L.dpx;
+        oy = (T)L.dpy;
+    }
     // dc in floatexp with one shared exponent.
-    const TE<T> cr = te_mulr(dxf, (T)L.dpx), ci = te_mulr(dyf, (T)L.dpy);
+    const TE<T> cr = te_mulr(dxf, ox), ci = te_mulr(dyf, oy);
     int e = (cr.m != T(0)) ? cr.e : ((ci.m != T(0)) ? ci.e : 0);
     if (cr.m != T(0) && ci.m != T(0)) e = imax(cr.e, ci.e);
     L.dce = e;
