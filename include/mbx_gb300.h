@@ -21,6 +21,7 @@ extern "C" {
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
 #define MBX_SUPER_SAMPLING 1
 #define MBX_EXTERIOR_DIST_EST 2
+#define MBX_NORMAL_MAP 16 /* value = smooth iteration; normal buffer = arg(z) - arg(dz/dc) (mp.cpp:375-378, 2489-2492, 3512-3515) */
 #define MBX_DE_OVERLAY 64
 
 /* What a request renders (ComputeMode, src/engine/compute_backend.h:18). */
@@ -60,7 +61,7 @@ typedef struct {
     int precision_mode;        /* MBX_PRECISION_* */
     int outputs_on_device;     /* 1: the three output pointers are CUDA device pointers */
     float* iterations;         /* required: smooth value / EDE distance / -2 interior / -10 empty */
-    float* normal;             /* optional: DE-overlay distance (MBX_DE_OVERLAY), else NULL */
+    float* normal;             /* optional: DE-overlay distance (MBX_DE_OVERLAY) or normal-map angle (MBX_NORMAL_MAP), else NULL */
     int32_t* escape_iteration; /* optional: escape iteration N per sample, -1 interior, -10 empty */
     volatile float* progress;  /* optional: 0..1 progress, written between passes */
     int reuse_reference;       /* 1: reuse the previous frame's reference orbit and BLA table when the view,

@@ -42,7 +42,7 @@ int validate(const mbx_request* r, std::string& why) {
     else if (r->compute_mode != MBX_MODE_MANDELBROT && r->compute_mode != MBX_MODE_JULIA) why = "unknown compute_mode";
     else if (r->compute_mode == MBX_MODE_JULIA && (r->sub != 1 || !r->fixed_c_re || !r->fixed_c_im || (r->coloring_method & ~MBX_EXTERIOR_DIST_EST) != 0))
         why = "Julia takes sub 1, the fixed c and coloring 0 or MBX_EXTERIOR_DIST_EST";
-    else if ((r->coloring_method & ~(MBX_SUPER_SAMPLING | MBX_EXTERIOR_DIST_EST | MBX_DE_OVERLAY)) != 0) why = "unsupported coloring_method bits";
+    else if ((r->coloring_method & ~(MBX_SUPER_SAMPLING | MBX_EXTERIOR_DIST_EST | MBX_NORMAL_MAP | MBX_DE_OVERLAY)) != 0) why = "unsupported coloring_method bits";
     else if (r->precision_mode != MBX_PRECISION_EXACT && r->precision_mode != MBX_PRECISION_MIXED) why = "unknown precision_mode";
     else if (!(r->bailout >= 0.0) || r->bailout > 1e18) why = "bailout must be in [0, 1e18]";
     else if ((long long)r->width * r->sub * r->height * r->sub > (1ll << 31) - 1) why = "frame too large";
@@ -320,7 +320,7 @@ int mbx_render_image(mbx_context* c, const mbx_request* r, const mbx_color_param
     if (v == MBX_OK) {
         if (r->sub != 1) why = "render_image takes sub 1 (supersampling is the colour pass's ss)";
         else if (r->width % p->supersample || r->height % p->supersample) why = "width and height must be multiples of supersample";
-        else if (p->shading == MBX_SHADE_NORMAL_MAP) why = "normal-map shading needs a normal-angle buffer the renderer does not produce; use mbx_colorize";
+        else if (p->shading == MBX_SHADE_NORMAL_MAP && !(r->coloring_method & MBX_NORMAL_MAP)) why = "normal-map shading needs MBX_NORMAL_MAP in coloring_method";
         else if (p->shading == MBX_SHADE_DE_OVERLAY && !(r->coloring_method & MBX_DE_OVERLAY)) why = "distance-overlay shading needs MBX_DE_OVERLAY in coloring_method";
         v = why.empty() ? MBX_OK : MBX_E_INVALID;
     }
@@ -335,7 +335,7 @@ int mbx_render_image(mbx_context* c, const mbx_request* r, const mbx_color_param
     if (!col) return MBX_E_NOMEM;
     const int ow = r->width / p->supersample, oh = r->height / p->supersample;
     const size_t samples = (size_t)r->width * r->height, pixels = (size_t)ow * oh;
-    const bool need_aux = p->shading == MBX_SHADE_DE_OVERLAY;
+    const bool need_aux = p->shading == MBX_SHADE_DE_OVERLAY || p->shading == MBX_SHADE_NORMAL_MAP;
     float *dv = nullptr, *da = nullptr;
     uint8_t* drgb = nullptr;
     std::string err;
@@ -346,9 +346,10 @@ int mbx_render_image(mbx_context* c, const mbx_request* r, const mbx_color_param
     }
     q.outputs_on_device = 1;
     q.iterations = dv;
-    q.normal = (r->coloring_method & MBX_DE_OVERLAY) ? da : nullptr;
-    if ((r->coloring_method & MBX_DE_OVERLAY) && !da) {
-        // the overlay buffer is computed even when the chosen shading ignores it
+    const bool wants_aux = (r->coloring_method & (MBX_DE_OVERLAY | MBX_NORMAL_MAP)) != 0;
+    q.normal = wants_aux ? da : nullptr;
+    if (wants_aux && !da) {
+        // the second buffer is computed even when the chosen shading ignores it
         rc = col->device_buffers(samples, pixels, true, &dv, &da, &drgb, err);
         if (rc != MBX_OK) {
             c->last_error = err;

@@ -1373,6 +1373,7 @@ FrameGeom Engine::geom() const {
     g.ede = (cm_ & 2) ? 1 : 0;
     g.deovl = (cm_ & 64) ? 1 : 0;
     g.deriv = deriv_ ? 1 : 0;
+    g.normal = (cm_ & 16) ? 1 : 0;
     return g;
 }
 
@@ -1815,7 +1816,7 @@ int Engine::compute_frame(const mbx_request& r) {
     MXIT_ = r.max_iterations;
     cm_ = r.coloring_method;
     mode_ = r.precision_mode;
-    deriv_ = (cm_ & (2 | 64)) != 0;
+    deriv_ = (cm_ & (2 | 16 | 64)) != 0; // EDE, normal map, DE overlay (mp.cpp:4190-4192)
     escf_ = (float)(r.bailout > 0 ? r.bailout : 1e8);
     ESC2_ = (double)(escf_ * escf_);
     const int full_h = r.full_height > 0 ? r.full_height : 0;
@@ -2175,7 +2176,7 @@ int Engine::render_shallow(volatile float* progress) {
     p.c0i = mpf_ld(c0_im_);
     p.dx = mpf_ld(dx_);
     p.dy = mpf_ld(dy_);
-    p.simd_semantics = (cm_ & 64) ? 0 : 1;
+    p.simd_semantics = (cm_ & (16 | 64)) ? 0 : 1; // the normal map and the DE overlay take the scalar path (mp.cpp:1455-1459)
     PixelSet g;
     g.keys = nullptr;
     g.grid_w = W_;
@@ -2212,6 +2213,7 @@ int Engine::shallow_samples(const std::vector<uint64_t>& samples) {
     ShallowParams p;
     p.g = geom();
     p.g.deovl = 0; // sub-samples carry the smooth/EDE value only (mp.cpp:1936-1967)
+    p.g.normal = 0;
     p.c0r = mpf_ld(c0_re_);
     p.c0i = mpf_ld(c0_im_);
     p.dx = mpf_ld(dx_);

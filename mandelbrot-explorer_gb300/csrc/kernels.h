@@ -124,6 +124,7 @@ struct FrameGeom {
     double ESC2;      // (double)(float R * float R) (mp.h:115-118)
     double dxf;       // mpf_get_ld(_dx)
     int ede, deovl, deriv;
+    int normal;       // normal map: arg(z) - arg(dz/dc) into the normal buffer (EDE takes precedence)
 };
 
 // Double-precision delta loop parameters (mp.cpp:2290-2585).

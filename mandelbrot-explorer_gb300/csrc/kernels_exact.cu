@@ -260,7 +260,12 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
                 v = (float)(sqrt(zrad) / g.dxf * log(zrad) / sqrt(dr * dr + di * di));
             } else {
                 v = (float)smooth_value(j + 1, zrad);
-                if (g.deovl && f.out.normal) f.out.normal[idx] = (float)(sqrt(zrad) / g.dxf * log(zrad) / sqrt(dr * dr + di * di));
+                if (g.normal) {
+                    // normal angle arg(z) - arg(dz/dc) (mp.cpp:2489-2492)
+                    if (f.out.normal) f.out.normal[idx] = (float)(atan2(zi, zr) - atan2(di, dr));
+                } else if (g.deovl && f.out.normal) {
+                    f.out.normal[idx] = (float)(sqrt(zrad) / g.dxf * log(zrad) / sqrt(dr * dr + di * di));
+                }
             }
             f.out.iter[idx] = v;
             if (f.out.escN) f.out.escN[idx] = j + 1;
@@ -615,7 +620,10 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 o.value = (float)fe_to_double(fe_div(fe_from(num), fe_mul(p.dxfe, Jmag)));
                 return o;
             }
-            if (g.deovl) {
+            if (g.normal) {
+                // normal angle arg(z) - arg(J); SJ > 0 (mp.cpp:3512-3515)
+                o.nrm = (float)(atan2(zi, zr) - atan2(ji, jr));
+            } else if (g.deovl) {
                 double num = sqrt(zrad) * log(zrad);
                 FE Jmag = fe_mul_d(SJ, sqrt(jr * jr + ji * ji));
                 o.nrm = (float)fe_to_double(fe_div(fe_from(num), fe_mul(p.dxfe, Jmag)));
@@ -853,7 +861,7 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
             atomicAdd(&f.ctr->gmp_flags, 1u);
         }
         f.out.iter[idx] = v;
-        if (g.deovl && f.out.normal) f.out.normal[idx] = o.nrm;
+        if ((g.deovl || g.normal) && f.out.normal) f.out.normal[idx] = o.nrm;
         if (f.out.escN) f.out.escN[idx] = o.state == 1 ? o.n : -1;
         f.out.done[i] = 1;
         if (o.state == 1) {
@@ -875,7 +883,7 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
 // kernel's per-lane arithmetic (mp.cpp:416-532).
 __device__ double shallow_scalar(double c_re, double c_im, int mxit, const FrameGeom& g, double* nrm, int* nout) {
     double z_re = c_re, z_im = c_im, d_re = 2, d_im = 0, dc_re = 1, dc_im = 0, tmp;
-    const bool deriv = g.ede || g.deovl;
+    const bool deriv = g.ede || g.deovl || g.normal;
     int i = 1;
     while (i < mxit) {
         tmp = 2.0 * (d_re * z_re - d_im * z_im);
@@ -893,6 +901,10 @@ __device__ double shallow_scalar(double c_re, double c_im, int mxit, const Frame
         if (tmp > g.ESC2) {
             *nout = i + 1;
             if (g.ede) return sqrt(tmp) * log(tmp) / sqrt(dc_re * dc_re + dc_im * dc_im);
+            if (g.normal) { // mp.cpp:375-378
+                if (nrm) *nrm = atan2(z_im, z_re) - atan2(dc_im, dc_re);
+                return (i + 1 - log(log(tmp) / 2 / kLn2) / kLn2);
+            }
             if (g.deovl && nrm) *nrm = sqrt(tmp) * log(tmp) / sqrt(dc_re * dc_re + dc_im * dc_im);
             return (i + 1 - log(log(tmp) / 2 / kLn2) / kLn2);
         }
@@ -1032,7 +1044,10 @@ __global__ void __launch_bounds__(128) k_shallow(DeviceFrame f, ShallowParams p)
         } else {
             double de = 0.0;
             val = shallow_scalar(cr, ci, g.mxit, g, &de, &nout);
-            if (g.deovl) {
+            if (g.normal) { // mp.cpp:1504-1507 (with EDE also set: the raw distance, angle 0)
+                f.out.iter[idx] = (float)val;
+                if (f.out.normal) f.out.normal[idx] = (float)de;
+            } else if (g.deovl) {
                 float v = (float)val;
                 f.out.iter[idx] = v;
                 if (f.out.normal) f.out.normal[idx] = (v < 0) ? 0.0f : (float)(de / p.dx);

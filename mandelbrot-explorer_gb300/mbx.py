@@ -31,6 +31,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libmbx_gb300.so")
 # ColoringMethod bits (src/engine/mandel_perturbation.h:30-49).
 SUPER_SAMPLING = 1
 EXTERIOR_DIST_EST = 2
+NORMAL_MAP = 16
 DE_OVERLAY = 64
 MODE_MANDELBROT, MODE_JULIA = 0, 1
 EMPTYPIXEL = -10.0
@@ -371,7 +372,7 @@ class CudaComputeBackend:
         n = req.sample_count()
         if req.iterations is None:
             req.iterations = np.empty(n, np.float32)
-        if req.normal is None and (req.coloring_method & DE_OVERLAY):
+        if req.normal is None and (req.coloring_method & (DE_OVERLAY | NORMAL_MAP)):
             req.normal = np.empty(n, np.float32)
         if req.escape_iteration is None and req.want_escape_iteration and isinstance(req.iterations, np.ndarray):
             req.escape_iteration = np.empty(n, np.int32)

@@ -35,7 +35,7 @@
 namespace {
 
 constexpr float EMPTY = -10.0f; // mp.h:23 EMPTYPIXEL
-constexpr int CM_SS = 1, CM_EDE = 2, CM_DEOVL = 64; // mp.h:30-49
+constexpr int CM_SS = 1, CM_EDE = 2, CM_NORMAL = 16, CM_DEOVL = 64; // mp.h:30-49
 constexpr int SA_N = 30;                            // mp.h:288
 
 // ---------------------------------------------------------------------------
@@ -429,7 +429,7 @@ class Engine {
         iter_[idx(p)] = v;
         if (escn_) escn_[idx(p)] = n;
     }
-    static bool deriv_of(int cm) { return (cm & (CM_EDE | CM_DEOVL)) != 0; }
+    static bool deriv_of(int cm) { return (cm & (CM_EDE | CM_NORMAL | CM_DEOVL)) != 0; }
 
     double floatPoint(double c_re, double c_im, int mxit, int cm, double* nrm, int* nout = nullptr) const;
     float shallowSimd(double cr, double ci, int mxit, int cm, int* nout = nullptr) const;
@@ -458,7 +458,8 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
     if (nout) *nout = -1;
     double z_re = c_re, z_im = c_im, d_re = 2, d_im = 0, dc_re = 1, dc_im = 0, tmp;
     const bool de_ovl = (cm & CM_DEOVL) != 0;
-    const bool deriv = (cm & CM_EDE) || de_ovl;
+    const bool normal = (cm & CM_NORMAL) != 0;
+    const bool deriv = (cm & CM_EDE) || normal || de_ovl;
     int i = 1;
     while (i < mxit) {
         tmp = 2.0 * (d_re * z_re - d_im * z_im);
@@ -476,6 +477,10 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
         if (tmp > ESC2) {
             if (nout) *nout = i + 1;
             if (cm & CM_EDE) return std::sqrt(tmp) * std::log(tmp) / std::sqrt(dc_re * dc_re + dc_im * dc_im);
+            if (normal) { // mp.cpp:375-378
+                if (nrm) *nrm = std::atan2((double)z_im, (double)z_re) - std::atan2((double)dc_im, (double)dc_re);
+                return (i + 1 - std::log(std::log(tmp) / 2 / std::log(2)) / std::log(2));
+            }
             if (de_ovl) {
                 if (nrm) *nrm = std::sqrt(tmp) * std::log(tmp) / std::sqrt(dc_re * dc_re + dc_im * dc_im);
                 return (i + 1 - std::log(std::log(tmp) / 2 / std::log(2)) / std::log(2));
@@ -1458,7 +1463,8 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
     double conf_D2 = 0, conf_zr = 0, conf_zi = 0;
     const bool ede = (cm & CM_EDE) != 0;
     const bool de_ovl = (cm & CM_DEOVL) != 0;
-    const bool deriv = ede || de_ovl;
+    const bool normal = (cm & CM_NORMAL) != 0;
+    const bool deriv = ede || normal || de_ovl;
     FE SJ{1.0, 0};
     double jr = 1.0, ji = 0.0, invSJd = 1.0;
     const bool detect_interior = use_interior;
@@ -1581,6 +1587,10 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
                 double num = std::sqrt(zrad) * std::log(zrad);
                 FE Jmag = fe_mul_d(SJ, std::sqrt(jr * jr + ji * ji));
                 return (float)fe_to_double(fe_div(fe_from(num), fe_mul(dxfe, Jmag)));
+            }
+            if (normal) { // mp.cpp:3512-3515
+                if (nrm) *nrm = (float)(std::atan2(zi, zr) - std::atan2(ji, jr));
+                return (float)((double)iter - std::log(std::log(zrad) / 2.0 / LG2) / LG2);
             }
             if (de_ovl) {
                 double num = std::sqrt(zrad) * std::log(zrad);
@@ -1778,7 +1788,8 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
     std::vector<double> glitch_p(n, -1.0);
     const bool ede = (cm & CM_EDE) != 0;
     const bool de_ovl = (cm & CM_DEOVL) != 0;
-    const bool deriv = ede || de_ovl;
+    const bool normal = (cm & CM_NORMAL) != 0;
+    const bool deriv = ede || normal || de_ovl;
     long long steps = 0, blas = 0, skipped = 0, gmp = 0;
     if (use_floatexp) {
         const bool noBla = !use_bla && !deriv;
@@ -1791,13 +1802,13 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
             FE Dci = fe_mul_d(dyfe, py - ref_y);
             float nrm = 0.0f;
             int nn = -1;
-            float value = noBla ? rescaledNoBla(Dcr, Dci, mx_ref_it, mxit, &nn) : pixelRescaled(Dcr, Dci, mx_ref_it, mxit, cm, de_ovl ? &nrm : nullptr, &nn);
+            float value = noBla ? rescaledNoBla(Dcr, Dci, mx_ref_it, mxit, &nn) : pixelRescaled(Dcr, Dci, mx_ref_it, mxit, cm, (normal || de_ovl) ? &nrm : nullptr, &nn);
             if (value == EMPTY || (fe_cutoff_sensitive && (value < 0 || value > mxit - 16))) {
                 value = accuratePixel(arr, mxit, cm, &nn);
                 ++gmp;
             }
             setPixel(arr, value, nn);
-            if (de_ovl && normal_) normal_[idx(arr)] = nrm;
+            if ((normal || de_ovl) && normal_) normal_[idx(arr)] = nrm;
             done[i] = 1;
         }
         stat_gmp += gmp;
@@ -1927,6 +1938,9 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
             if (zrad > ESC2) {
                 if (ede) {
                     setPixel(arr, std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di), j + 1);
+                } else if (normal) { // mp.cpp:2489-2492
+                    setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
+                    if (normal_) normal_[idx(arr)] = (float)(std::atan2((double)zi, (double)zr) - std::atan2((double)di, (double)dr));
                 } else if (de_ovl) {
                     setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
                     if (normal_) normal_[idx(arr)] = (float)(std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di));
@@ -2109,13 +2123,19 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
         double c0r = mpf_ld(c0_re), c0i = mpf_ld(c0_im), dxf = mpf_ld(dx), dyf = mpf_ld(dy);
         const bool ede = (cm & CM_EDE) != 0;
         const bool deovl = (cm & CM_DEOVL) != 0;
+        const bool nmap = (cm & CM_NORMAL) != 0;
 #pragma omp parallel for schedule(dynamic, 1)
         for (int i = 0; i < H; ++i) {
             double cim = c0i + dyf * i;
             for (int j = 0; j < W; ++j) {
                 Pix p{{i, j, 0, 0}};
                 int nn = -1;
-                if (!deovl) {
+                if (nmap) { // mp.cpp:1504-1507
+                    double nv = 0.0;
+                    iter_[idx(p)] = (float)floatPoint(c0r + dxf * j, cim, mxit, cm, &nv, &nn);
+                    if (escn_) escn_[idx(p)] = nn;
+                    if (normal_) normal_[idx(p)] = (float)nv;
+                } else if (!deovl) {
                     double val = shallowSimd(c0r + dxf * j, cim, mxit, cm, &nn);
                     if (ede && val >= 0) val /= dxf;
                     iter_[idx(p)] = (float)val;

@@ -123,3 +123,17 @@ def test_invalid_color_requests(be):
         be.render_image(req, mbx.ColorParams(supersample=3))
     with pytest.raises(RuntimeError):  # no overlay buffer requested
         be.render_image(mbx.ComputeRequest("-0.75", "0.1", "10", 96, 60, 500), mbx.ColorParams(shading=mbx.SHADE_DE_OVERLAY))
+
+
+def test_render_image_normal_map_matches_reference_tool(be):
+    """MANDEL_NORMAL=1 end to end: the renderer's normal-map angles (exact form)
+    shaded on the device, against the oracle colouring the same buffers."""
+    v = dict(center_re="-0.74364388703715", center_im="0.13182590420533", scale="100000", max_iterations=3000)
+    ss = 2
+    w, h = 96 * ss, 54 * ss
+    p = mbx.ColorParams(supersample=ss, shading=mbx.SHADE_NORMAL_MAP, light_el=0.9)
+    img = be.render_image(mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], w, h, v["max_iterations"], coloring_method=mbx.NORMAL_MAP), p)
+    req = mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], w, h, v["max_iterations"], coloring_method=mbx.NORMAL_MAP)
+    assert be.compute_status(req) == mbx.OK, be.last_error()
+    want = oracle.colorize(req.iterations, w // ss, h // ss, ss, aux=req.normal, mapping=0, shading=mbx.SHADE_NORMAL_MAP, density=60.0, light_az=2.3, light_el=0.9, relief_strength=1.0, de_k=1.5)
+    _agree(img, want)

@@ -89,7 +89,7 @@ def test_mixed_on_parity_cases(backend):
             r[mode] = (req.iterations, req.escape_iteration, backend.last_stats.as_dict())
         mi, mn, mst = r[mbx.PRECISION_MIXED]
         ei, en, _ = r[mbx.PRECISION_EXACT]
-        if c["coloring_method"] & (2 | 64):
+        if c["coloring_method"] & (2 | 16 | 64):
             assert np.array_equal(mi, ei) and np.array_equal(mn, en), name
             print("\n[mixed vs exact] %s: DE colouring, exact form used" % name)
             continue

@@ -45,7 +45,7 @@ def test_exact_matches_oracle(backend, name):
     it, nr, en, st = gpu_render(backend, c)
     oit, onr, oen, ost = oracle.render(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"])
     assert_same(it, en, oit, oen, name)
-    if c["coloring_method"] & 64:
+    if c["coloring_method"] & (16 | 64):
         np.testing.assert_allclose(nr, onr, rtol=RTOL, atol=0)
     assert st["kernel_launches"] > 0 and st["samples"] > 0
 
