@@ -6,6 +6,8 @@
 //   gate -> main: FP32, double-float, FP64 lane passes -> counters to the host.
 #include "batch.h"
 
+#include <thread>
+
 #include <algorithm>
 #include <cstring>
 
@@ -270,12 +272,26 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
     std::vector<BatchSlot> slots(n);
     std::vector<mbx_stats> vst(n);
     for (int i = 0; i < n; ++i) slots[i].want_cost = schedule_ != 0;
-    for (int i = 0; i < n; ++i) {
-        rc = eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
-        if (rc != MBX_OK) {
-            err = eng_[i]->error();
-            return rc;
-        }
+    {
+        // The frames' host work (GMP reference orbits, nucleus searches) is
+        // independent per engine: up to `lanes` engines build concurrently,
+        // each thread with its own product helpers (up to seven threads each
+        // while a loop runs), so the lane count follows the host's cores.
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int lanes = std::max(1, std::min({n, 4, (int)(hw / 7)}));
+        std::vector<int> rcs((size_t)n, MBX_OK);
+        auto work = [&](int t) {
+            for (int i = t; i < n; i += lanes) rcs[(size_t)i] = eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < lanes; ++t) th.emplace_back(work, t);
+        work(0);
+        for (auto& x : th) x.join();
+        for (int i = 0; i < n; ++i)
+            if (rcs[(size_t)i] != MBX_OK) {
+                err = eng_[i]->error();
+                return rcs[(size_t)i];
+            }
     }
     std::vector<int> deferred;
     for (int i = 0; i < n; ++i)

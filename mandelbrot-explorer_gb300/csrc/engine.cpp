@@ -49,7 +49,6 @@ inline int exp_floor_log2(double x) {
 
 struct MpfTemp {
     mpf_t v;
-    MpfTemp() { mpf_init(v); }
     explicit MpfTemp(mp_bitcnt_t p) { mpf_init2(v, p); }
     ~MpfTemp() { mpf_clear(v); }
     operator mpf_ptr() { return v; }
@@ -308,9 +307,9 @@ void Engine::reset_cancel() {
 
 void Engine::set_precision(int p) { // mp.cpp:2030-2045
     if (!mpf_ready_) {
-        mpf_init(c0_re_); mpf_init(c0_im_); mpf_init(dx_); mpf_init(dy_); mpf_init(scale_);
-        mpf_init(ref_re_); mpf_init(ref_im_); mpf_init(t1_); mpf_init(t2_);
-        for (int i = 0; i < 2; ++i) { mpf_init(zre_[i]); mpf_init(zim_[i]); }
+        mpf_init2(c0_re_, p); mpf_init2(c0_im_, p); mpf_init2(dx_, p); mpf_init2(dy_, p); mpf_init2(scale_, p);
+        mpf_init2(ref_re_, p); mpf_init2(ref_im_, p); mpf_init2(t1_, p); mpf_init2(t2_, p);
+        for (int i = 0; i < 2; ++i) { mpf_init2(zre_[i], p); mpf_init2(zim_[i], p); }
         mpf_ready_ = true;
     }
     mpf_set_prec(c0_re_, p); mpf_set_prec(c0_im_, p); mpf_set_prec(dx_, p); mpf_set_prec(dy_, p);
@@ -510,7 +509,8 @@ float Engine::gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) c
 }
 
 float Engine::gmp_sample(const int* a, int mxit, int* nout) const { // mp.cpp:896-919
-    MpfTemp cre, cim, off, soff;
+    const mp_bitcnt_t pr = mpf_get_prec(c0_re_);
+    MpfTemp cre(pr), cim(pr), off(pr), soff(pr);
     mpf_set(cre, c0_re_);
     mpf_set(cim, c0_im_);
     mpf_mul_ui(off, dx_, a[1]);
@@ -531,7 +531,8 @@ float Engine::gmp_sample(const int* a, int mxit, int* nout) const { // mp.cpp:89
 }
 
 bool Engine::ref_tail_escapes(int last, int extra) { // mp.cpp:927-957
-    MpfTemp zr, zi, a1, a2;
+    const mp_bitcnt_t pr = mpf_get_prec(c0_re_);
+    MpfTemp zr(pr), zi(pr), a1(pr), a2(pr);
     if (use_fixed_) {
         fz_re_[last & 1].to_mpf(zr);
         fz_im_[last & 1].to_mpf(zi);
@@ -1311,7 +1312,7 @@ int Engine::build_dc_tables() {
     const int nx = xmax - xmin + 1, ny = ymax - ymin + 1;
     hdcx_.resize(nx);
     hdcy_.resize(ny);
-    MpfTemp a;
+    MpfTemp a(mpf_get_prec(dx_));
     for (int x = xmin; x <= xmax; ++x) {
         mpf_mul_ui(a, dx_, std::abs(x));
         if (x < 0) mpf_neg(a, a);
@@ -1829,7 +1830,9 @@ int Engine::compute_frame(const mbx_request& r) {
             if (ch >= '0' && ch <= '9') ++digits;
         prec = (int)(digits * std::log(10) / std::log(2)) + 64;
     }
-    mpf_set_default_prec((mp_bitcnt_t)prec);
+    // Every mpf value of a frame takes this precision explicitly (the library
+    // never relies on GMP's process-wide default), so engines may build their
+    // references concurrently.
     set_precision(prec);
     {
         char buf[256];
@@ -1838,7 +1841,7 @@ int Engine::compute_frame(const mbx_request& r) {
         reuse_ = r.reuse_reference && cache_.valid && cache_.key == frame_key_;
         if (!reuse_) cache_.valid = false;
     }
-    MpfTemp cre, cim, msc;
+    MpfTemp cre(prec), cim(prec), msc(prec);
     if (mpf_set_str(cre, r.center_re, 10) != 0 || mpf_set_str(cim, r.center_im, 10) != 0 || mpf_set_str(msc, r.scale, 10) != 0 || mpf_sgn(msc) <= 0) {
         err_ = "unparsable centre or scale";
         return MBX_E_INVALID;
@@ -1899,7 +1902,8 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     mpf_set(scale_, scale);
     const int rows = (full_h > 0) ? full_h : H_;
     {
-        MpfTemp dw, dh;
+        const mp_bitcnt_t pr = mpf_get_prec(c0_re_);
+        MpfTemp dw(pr), dh(pr);
         mpf_set_ui(dw, 2);
         mpf_div(dw, dw, scale);
         mpf_set(dh, dw);
@@ -1912,7 +1916,7 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
         mpf_div_ui(dy_, dh, rows - 1);
         mpf_mul_ui(dy_, dy_, 2);
         if (row_base > 0) {
-            MpfTemp off;
+            MpfTemp off(pr);
             mpf_mul_ui(off, dy_, row_base);
             mpf_add(c0_im_, c0_im_, off);
         }
@@ -2112,14 +2116,15 @@ int Engine::render_julia(mpf_ptr z_re, mpf_ptr z_im, mpf_ptr scale, const char* 
     use_floatexp_ = false;
     ref_period_ = 0;
     const int rows = full_h > 0 ? full_h : H_;
-    MpfTemp cr, ci;
+    const mp_bitcnt_t pr = mpf_get_prec(c0_re_);
+    MpfTemp cr(pr), ci(pr);
     if (mpf_set_str(cr, fcr, 10) != 0 || mpf_set_str(ci, fci, 10) != 0) {
         err_ = "unparsable fixed c";
         return MBX_E_INVALID;
     }
     mpf_set(scale_, scale);
     {
-        MpfTemp dw, dh;
+        MpfTemp dw(pr), dh(pr);
         mpf_set_ui(dw, 2);
         mpf_div(dw, dw, scale);
         mpf_set(dh, dw);

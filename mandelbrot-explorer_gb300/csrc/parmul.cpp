@@ -8,8 +8,10 @@
 
 namespace mbx {
 
+// One pool per calling thread: engines building references on different
+// threads (a batch) each get their own helpers.
 ParMul& ParMul::instance() {
-    static ParMul p;
+    thread_local ParMul p;
     return p;
 }
 
