@@ -236,7 +236,7 @@ class Engine {
 
     // mixed-pass launch shape (set by the autotuner / defaults)
     int mixed_threads_ = 256;
-    int mixed_blocks_per_sm_ = 2;
+    int mixed_blocks_per_sm_ = 3;
     int smem_orbit_limit_ = 200 * 1024;
     float mixed_wmax2_ = 1e16f;
 

@@ -73,7 +73,7 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
 // LANES < 32: only the low LANES lanes of a warp take samples. The rerun
 // passes are latency-bound (few samples, long dependency chains), so spreading
 // their samples over more warps hides more latency than filling each warp.
-template <class T, int MAXT, int MINB, int LANES = 32>
+template <class T, int MAXT, int MINB, int LANES = 32, bool INTR = true>
 __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedParams p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orbit) {
     using V2 = typename LaneReal<T>::V2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         if (__ballot_sync(0xffffffffu, live) == 0) break;
         if (live) {
             T zrad = T(0);
-            const int st = lane_run(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase);
+            const int st = lane_run<T, INTR>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 // smooth value N - log2(log2|z|) in the lane type (the output is FP32)
@@ -446,6 +446,10 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
         kern<<<blocks, threads, smem, st_>>>(g, p, dbla32_.p, dZf_.p);
         return cudaGetLastError();
     };
+    if (!p.use_interior) { // exterior after the probe: the lane without interior detectors
+        if (mixed_blocks_per_sm_ >= 3) return launch(k_lane_pass<float, 256, 3, 32, false>);
+        return launch(k_lane_pass<float, 256, 2, 32, false>);
+    }
     if (mixed_blocks_per_sm_ >= 4) return launch(k_lane_pass<float, 256, 4>);
     if (mixed_blocks_per_sm_ == 3) return launch(k_lane_pass<float, 256, 3>);
     return launch(k_lane_pass<float, 256, 2>);
@@ -491,7 +495,7 @@ cudaError_t Engine::run_rerun_pass(const DeviceFrame& f) {
 // Batched passes (one FP32 launch over all views, then the two rerun tiers).
 cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st) {
     if (tier == 0) {
-        k_batch_pass<float, 256, 2><<<nsm * 2, 256, 0, st>>>(a);
+        k_batch_pass<float, 256, 3><<<nsm * 3, 256, 0, st>>>(a);
     } else if (tier == 1) {
         BatchArgs b = a;
         b.wide_from = kWideLanesPerSm * (unsigned)nsm;

@@ -498,7 +498,10 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 // Advance one lane by up to `budget` iterations. Returns 0 running, 1 escaped,
 // 2 interior, 3 precision spent (FP32 lane only: rerun in FP64); zrad_out is
 // set on escape.
-template <class T>
+// INTR = false compiles the lane without its interior detectors, for passes
+// whose interior detection is off (exterior frames after the probe): their
+// state then takes no registers.
+template <class T, bool INTR = true>
 MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
                      int reflen, T ESC2f, int blamask, T& zrad_out, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip,
                      unsigned long long& n_rebase) {
@@ -513,7 +516,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
     for (int b = 0; b < budget; ++b) {
         if (L.iter >= g.mxit) return lane_interior(L);
-        if (p.use_interior) {
+        if (INTR && p.use_interior) {
             const int idxs = per ? L.rm : L.m;
             if (idxs == L.sidx && L.wr == L.swr && L.wi == L.swi && L.S.m == L.sS.m && L.S.e == L.sS.e) return lane_interior(L);
             if (L.iter - L.save_iter2 >= L.twin2) {
@@ -621,7 +624,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 return 1;
             }
         }
-        if (p.use_interior) {
+        if (INTR && p.use_interior) {
             if (L.conf_P > 0) {
                 L.conf_D2 *= 4.0f * (float)zrad;
                 if (L.conf_D2 > 1e18f) L.conf_D2 = 1e18f;

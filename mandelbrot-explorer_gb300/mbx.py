@@ -355,7 +355,7 @@ class CudaComputeBackend:
             raise RuntimeError("autotune failed (%d): %s" % (rc, self.last_error()))
         return t.as_dict()
 
-    def set_tuning(self, threads=256, blocks_per_sm=2, smem_orbit_limit=200 * 1024, rescale_window=1e16):
+    def set_tuning(self, threads=256, blocks_per_sm=3, smem_orbit_limit=200 * 1024, rescale_window=1e16):
         rc = self._lib.mbx_set_tuning(self._ctx, threads, blocks_per_sm, smem_orbit_limit, rescale_window)
         if rc != OK:
             raise RuntimeError("set_tuning failed (%d)" % rc)
