@@ -1877,10 +1877,6 @@ int Engine::compute_frame(const mbx_request& r) {
         reuse_ = false;
         rc = render_julia(cre, cim, msc, r.fixed_c_re, r.fixed_c_im, full_h, row_base);
     } else {
-        hZ_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
-        hzm3_.assign((size_t)MXIT_ + 2, 0.0);
-        hD_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
-        hZfe_.assign((size_t)MXIT_ + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
         rc = render(cre, cim, msc, full_h, row_base, r.progress);
     }
     if (batch_slot_ && batch_slot_->deferred) return rc; // passes and readback follow in the batch
@@ -1937,8 +1933,14 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     int rc = MBX_OK;
     refs_built_in_frame_ = 0;
     if (reuse_ && restore_cache(&ref_it)) {
-        stats_.reused_reference = 1;
+        stats_.reused_reference = 1; // the host orbit shadows still hold this reference
     } else {
+        // host orbit shadows, up to maxiter + 1 entries (tens of MB at maxiter
+        // 1e6): cleared only when a reference is built
+        hZ_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
+        hzm3_.assign((size_t)MXIT_ + 2, 0.0);
+        hD_.assign((size_t)MXIT_ + 2, make_double2(0, 0));
+        hZfe_.assign((size_t)MXIT_ + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
         ref_it = reference_for_frame();
         if (cancel_.load()) return MBX_E_CANCELLED;
         stats_.reference_length = ref_period_ > 0 ? ref_period_ : ref_it;
