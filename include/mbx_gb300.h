@@ -88,6 +88,8 @@ typedef struct {
     double rerun_gpu_ms;            /* device time of the reruns (included in pass_gpu_ms) */
     long long fp64_reruns_fp64;     /* of those, samples rerun again in FP64 (double-float estimate too large) */
     double rerun_fp64_gpu_ms;       /* device time of the FP64 reruns (included in rerun_gpu_ms) */
+    long long exact_steps;          /* mixed form: steps taken in FP64 floatexp (orbit or delta below FP32's range) */
+    long long fe_rebases;           /* mixed form: rebases decided in FP64 floatexp (inside the margin, end of reference) */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns

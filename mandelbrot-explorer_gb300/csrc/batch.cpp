@@ -357,6 +357,8 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             bs.effective_iterations += (long long)k.effective_iters;
             bs.interior += (int)k.interior;
             bs.rebases += (long long)k.rebases;
+            bs.exact_steps += (long long)k.exact_steps;
+            bs.fe_rebases += (long long)k.fe_rebases;
         }
         bs.fp64_reruns = (long long)h_ctr_[0].rerun_n + h_ctr_[3].rerun_n;
         bs.fp64_reruns_fp64 = (long long)h_ctr_[1].rerun_n + h_ctr_[4].rerun_n;

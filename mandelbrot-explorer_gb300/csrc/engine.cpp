@@ -1475,6 +1475,8 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         a.interior += b.interior; // callers read the pass's interior count from hctr_
     }
     stats_.rebases += (long long)a.rebases;
+    stats_.exact_steps += (long long)a.exact_steps;
+    stats_.fe_rebases += (long long)a.fe_rebases;
     stats_.steps += (long long)a.steps;
     stats_.bla_applies += (long long)a.bla_applies;
     stats_.bla_skipped += (long long)a.bla_skipped;

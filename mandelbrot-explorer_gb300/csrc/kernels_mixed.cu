@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     const BlaEntry<T>* bt = f.bla.use ? blat : nullptr;
     const TE<T> dxf = te_from_fe<T>(p.dxfe), dyf = te_from_fe<T>(p.dyfe);
     const unsigned lane_id = threadIdx.x & 31;
-    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0;
+    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
     unsigned cost0 = 0;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         if (__ballot_sync(0xffffffffu, live) == 0) break;
         if (live) {
             T zrad = T(0);
-            const int st = lane_run<T, INTR>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase);
+            const int st = lane_run<T, INTR>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 // smooth value N - log2(log2|z|) in the lane type (the output is FP32)
@@ -172,6 +172,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     atomicAdd(&f.ctr->bla_skipped, n_skip);
     atomicAdd(&f.ctr->effective_iters, n_eff);
     atomicAdd(&f.ctr->rebases, n_rebase);
+    atomicAdd(&f.ctr->exact_steps, n_exact);
+    atomicAdd(&f.ctr->fe_rebases, n_ferebase);
     atomicAdd(&f.ctr->finished, n_fin);
     atomicAdd(&f.ctr->interior, n_int);
 }
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     if ((unsigned long long)blockIdx.x * (MAXT / 32) * LANES >= n) return;
     const unsigned take = LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u);
     const unsigned lane_id = threadIdx.x & 31;
-    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0;
+    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
     int view = 0;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
             const BlaEntry<T>* bt = vd.f.bla.use ? ViewTables<T>::bla(vd) : nullptr;
             T zrad = T(0);
             const int st = lane_run(L, 32, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, (T)vd.p.g.ESC2, (1 << vd.f.bla.minlevel) - 1, zrad,
-                                    n_steps, n_bla, n_skip, n_rebase);
+                                    n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (st != 0 && vd.f.out.cost) vd.f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 vd.f.out.iter[L.oidx] = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
@@ -300,6 +302,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     atomicAdd(&a.ctr->bla_skipped, n_skip);
     atomicAdd(&a.ctr->effective_iters, n_eff);
     atomicAdd(&a.ctr->rebases, n_rebase);
+    atomicAdd(&a.ctr->exact_steps, n_exact);
+    atomicAdd(&a.ctr->fe_rebases, n_ferebase);
     atomicAdd(&a.ctr->finished, n_fin);
     atomicAdd(&a.ctr->interior, n_int);
 }

@@ -15,6 +15,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <climits>
+#include <type_traits>
+
 #include "dfloat.cuh"
 #include "kernels.h"
 
@@ -231,6 +234,57 @@ MBX_HDF void exact_step(FE Xr, FE Xi, FE dcr, FE dci, FE& S, double& wr, double&
     S = fe_renorm(mag, e);
     wr = nr / mag;
     wi = ni / mag;
+}
+
+// The FP32 lane's rare steps in FP32 floatexp (float mantissa, int exponent):
+// the floatexp step of exact_step with one shared exponent, and the sum
+// X + S w with the components kept as mantissa/exponent pairs. The FP32 lane's
+// error estimate covers their float roundings like any other step's, so they
+// need no FP64 (whose warp instructions cost ~60 FP32 ones on this part).
+MBX_HD F32E te_from_fe_f(FE a) { return a.m == 0.0 ? F32E{0.0f, 0} : te_norm((float)a.m, (int)a.e); }
+MBX_HD float te_align_f(float m, int me, int e) { // m 2^me in units of 2^e (e >= me - 30 assumed)
+    const int d = me - e;
+    if (m == 0.0f || d < -30) return 0.0f;
+    return ldexp_ftz(m, d);
+}
+MBX_HD void exact_step_f(F32E Xr, F32E Xi, F32E dcr, F32E dci, F32E& S, float& wr, float& wi) {
+    const float sm = S.m, sm2 = sm * sm;
+    const int se = S.e;
+    int e = INT_MIN;
+    const bool has_w = wr != 0.0f || wi != 0.0f;
+    if (has_w && Xr.m != 0.0f) e = imax(e, Xr.e + se);
+    if (has_w && Xi.m != 0.0f) e = imax(e, Xi.e + se);
+    if (has_w) e = imax(e, se + se);
+    if (dcr.m != 0.0f) e = imax(e, dcr.e);
+    if (dci.m != 0.0f) e = imax(e, dci.e);
+    if (e == INT_MIN) {
+        S = F32E{0.5f, 1};
+        wr = wi = 0.0f;
+        return;
+    }
+    const float xs_r = te_align_f(Xr.m * sm, Xr.e + se, e);
+    const float xs_i = te_align_f(Xi.m * sm, Xi.e + se, e);
+    const float s2 = te_align_f(sm2, se + se, e);
+    const float cr = te_align_f(dcr.m, dcr.e, e);
+    const float ci = te_align_f(dci.m, dci.e, e);
+    const float nr = 2.0f * (xs_r * wr - xs_i * wi) + s2 * (wr * wr - wi * wi) + cr;
+    const float ni = 2.0f * (xs_r * wi + xs_i * wr) + 2.0f * s2 * wr * wi + ci;
+    const float mag = sqrtf(nr * nr + ni * ni);
+    if (mag == 0.0f) {
+        S = F32E{0.5f, 1};
+        wr = wi = 0.0f;
+        return;
+    }
+    S = te_norm(mag, e);
+    wr = nr / mag;
+    wi = ni / mag;
+}
+// z = X + S w per component as F32E.
+MBX_HD F32E te_add_f(F32E a, F32E b) {
+    if (a.m == 0.0f) return b;
+    if (b.m == 0.0f) return a;
+    const int e = imax(a.e, b.e);
+    return te_norm(te_align_f(a.m, a.e, e) + te_align_f(b.m, b.e, e), e);
 }
 
 // Floatexp copy of the FP64 BLA table: A and B as mantissa pairs with one
@@ -504,7 +558,7 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 template <class T, bool INTR = true>
 MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
                      int reflen, T ESC2f, int blamask, T& zrad_out, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip,
-                     unsigned long long& n_rebase) {
+                     unsigned long long& n_rebase, unsigned long long& n_exact, unsigned long long& n_ferebase) {
     using R = LaneReal<T>;
     using Z = typename R::Z;
     const FrameGeom& g = p.g;
@@ -573,7 +627,29 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 const float a = R::tof(nwr), c = R::tof(nwi);
                 L.err2 = L.err2 * L.g2 + R::kEps2 * (a * a + c * c);
             }
+        } else if constexpr (std::is_same<T, float>::value) {
+            ++n_exact;
+            const F32E S0 = L.S;
+            const F32E zero{0.0f, 0};
+            const F32E Xr = L.m ? te_from_fe_f(Zfe[L.rm].re) : zero, Xi = L.m ? te_from_fe_f(Zfe[L.rm].im) : zero;
+            F32E S = S0;
+            float wr = L.wr, wi = L.wi;
+            exact_step_f(Xr, Xi, te_norm(L.dcm.x, L.dce), te_norm(L.dcm.y, L.dce), S, wr, wi);
+            if (R::kTrackError) {
+                // error carried into the new units: |2 z|^2 (S0 / S)^2 err2, z = X + S0 w
+                const F32E zr = te_add_f(Xr, te_norm(S0.m * L.wr, S0.e)), zi = te_add_f(Xi, te_norm(S0.m * L.wi, S0.e));
+                const int ez = zr.m == 0.0f ? zi.e : (zi.m == 0.0f ? zr.e : imax(zr.e, zi.e));
+                const float mr = te_align_f(zr.m, zr.e, ez), mi = te_align_f(zi.m, zi.e, ez);
+                const float q = S.m == 0.0f ? 0.0f : S0.m / S.m;
+                const float amp = ldexp_ftz(4.0f * (mr * mr + mi * mi) * q * q, imax(-300, imin(300, 2 * ez + 2 * (S0.e - S.e))));
+                L.err2 = fminf(amp * L.err2, 3e38f) + R::kEps2;
+            }
+            L.S = S;
+            L.wr = wr;
+            L.wi = wi;
+            lane_refresh(L);
         } else {
+            ++n_exact;
             double wr = (double)L.wr, wi = (double)L.wi;
             const FE S0 = fe_from_te(L.S);
             FE S = S0;
@@ -720,7 +796,44 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
             L.rm = -1;
             L.Xc = R::make2(T(0), T(0));
             ++n_rebase;
+        } else if (decide == 2 && std::is_same<T, float>::value) {
+            // the decision and the new delta in FP32 floatexp: z = X + S w
+            // per component, |z| against |dz| on mantissa/exponent pairs
+            ++n_ferebase;
+            const F32E zero{0.0f, 0};
+            const F32E Xr = L.m ? te_from_fe_f(Zfe[L.rm].re) : zero, Xi = L.m ? te_from_fe_f(Zfe[L.rm].im) : zero;
+            const float Sm = R::tof(L.S.m), wrf = R::tof(L.wr), wif = R::tof(L.wi);
+            const F32E zr = te_add_f(Xr, te_norm(Sm * wrf, L.S.e)), zi = te_add_f(Xi, te_norm(Sm * wif, L.S.e));
+            const int ez = zr.m == 0.0f ? zi.e : (zi.m == 0.0f ? zr.e : imax(zr.e, zi.e));
+            const float mr = te_align_f(zr.m, zr.e, ez), mi = te_align_f(zi.m, zi.e, ez);
+            const float mz = sqrtf(mr * mr + mi * mi);
+            const F32E zn = te_norm(mz, ez), dn = te_norm(fabsf(Sm) * sqrtf(wrf * wrf + wif * wif), L.S.e);
+            const bool smaller = zn.m == 0.0f ? dn.m != 0.0f : (dn.m != 0.0f && (zn.e < dn.e || (zn.e == dn.e && zn.m < dn.m)));
+            if ((!per && L.m >= reflen) || smaller) {
+                if (mz == 0.0f) {
+                    L.wr = L.wi = T(0);
+                } else {
+                    L.S = TE<T>{T(zn.m), zn.e};
+                    L.wr = T(mr / mz);
+                    L.wi = T(mi / mz);
+                    lane_refresh(L);
+                    if (R::kTrackError) {
+                        // plus the roundings of X + dz in float, relative to |z|:
+                        // (|X|^2 + |dz|^2) / |z|^2 times the per-step variance
+                        const int ex = Xr.m == 0.0f ? Xi.e : (Xi.m == 0.0f ? Xr.e : imax(Xr.e, Xi.e));
+                        const float ar = te_align_f(Xr.m, Xr.e, ex), ai = te_align_f(Xi.m, Xi.e, ex);
+                        const float cx = (Xr.m == 0.0f && Xi.m == 0.0f) ? 0.0f : ldexp_ftz((ar * ar + ai * ai) / (mz * mz), imax(-300, imin(300, 2 * (ex - ez))));
+                        const float cd = ldexp_ftz(Sm * Sm * (wrf * wrf + wif * wif) / (mz * mz), imax(-300, imin(300, 2 * (S0.e - ez))));
+                        L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2 * (1.0f + fminf(cx + cd, 1e30f));
+                    }
+                }
+                L.m = 0;
+                L.rm = -1;
+                L.Xc = R::make2(T(0), T(0));
+                ++n_rebase;
+            }
         } else if (decide == 2) {
+            ++n_ferebase;
             const FE S = fe_from_te(L.S);
             FE Xmr = L.m ? Zfe[L.rm].re : fe_make(0.0, 0);
             FE Xmi = L.m ? Zfe[L.rm].im : fe_make(0.0, 0);

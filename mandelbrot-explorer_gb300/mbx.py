@@ -110,6 +110,8 @@ class Stats(ctypes.Structure):
         ("rerun_gpu_ms", ctypes.c_double),
         ("fp64_reruns_fp64", ctypes.c_longlong),
         ("rerun_fp64_gpu_ms", ctypes.c_double),
+        ("exact_steps", ctypes.c_longlong),
+        ("fe_rebases", ctypes.c_longlong),
     ]
 
     def as_dict(self):
