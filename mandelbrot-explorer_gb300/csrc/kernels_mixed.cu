@@ -105,7 +105,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     const BlaEntry<T>* bt = f.bla.use ? blat : nullptr;
     const TE<T> dxf = te_from_fe<T>(p.dxfe), dyf = te_from_fe<T>(p.dyfe);
     const unsigned lane_id = threadIdx.x & 31;
-    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    // per-thread counts of one pass (32-bit: a thread executes far fewer than
+    // 2^32 steps per pass); skipped and effective iterations stay 64-bit
+    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    unsigned long long n_skip = 0, n_eff = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
     unsigned cost0 = 0;
@@ -167,13 +170,13 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
             live = false;
         }
     }
-    atomicAdd(&f.ctr->steps, n_steps);
-    atomicAdd(&f.ctr->bla_applies, n_bla);
+    atomicAdd(&f.ctr->steps, (unsigned long long)n_steps);
+    atomicAdd(&f.ctr->bla_applies, (unsigned long long)n_bla);
     atomicAdd(&f.ctr->bla_skipped, n_skip);
     atomicAdd(&f.ctr->effective_iters, n_eff);
-    atomicAdd(&f.ctr->rebases, n_rebase);
-    atomicAdd(&f.ctr->exact_steps, n_exact);
-    atomicAdd(&f.ctr->fe_rebases, n_ferebase);
+    atomicAdd(&f.ctr->rebases, (unsigned long long)n_rebase);
+    atomicAdd(&f.ctr->exact_steps, (unsigned long long)n_exact);
+    atomicAdd(&f.ctr->fe_rebases, (unsigned long long)n_ferebase);
     atomicAdd(&f.ctr->finished, n_fin);
     atomicAdd(&f.ctr->interior, n_int);
 }
@@ -214,7 +217,10 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     if ((unsigned long long)blockIdx.x * (MAXT / 32) * LANES >= n) return;
     const unsigned take = LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u);
     const unsigned lane_id = threadIdx.x & 31;
-    unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    // per-thread counts of one pass (32-bit: a thread executes far fewer than
+    // 2^32 steps per pass); skipped and effective iterations stay 64-bit
+    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    unsigned long long n_skip = 0, n_eff = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
     int view = 0;
@@ -297,13 +303,13 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
             live = false;
         }
     }
-    atomicAdd(&a.ctr->steps, n_steps);
-    atomicAdd(&a.ctr->bla_applies, n_bla);
+    atomicAdd(&a.ctr->steps, (unsigned long long)n_steps);
+    atomicAdd(&a.ctr->bla_applies, (unsigned long long)n_bla);
     atomicAdd(&a.ctr->bla_skipped, n_skip);
     atomicAdd(&a.ctr->effective_iters, n_eff);
-    atomicAdd(&a.ctr->rebases, n_rebase);
-    atomicAdd(&a.ctr->exact_steps, n_exact);
-    atomicAdd(&a.ctr->fe_rebases, n_ferebase);
+    atomicAdd(&a.ctr->rebases, (unsigned long long)n_rebase);
+    atomicAdd(&a.ctr->exact_steps, (unsigned long long)n_exact);
+    atomicAdd(&a.ctr->fe_rebases, (unsigned long long)n_ferebase);
     atomicAdd(&a.ctr->finished, n_fin);
     atomicAdd(&a.ctr->interior, n_int);
 }
@@ -451,7 +457,8 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
         return cudaGetLastError();
     };
     if (!p.use_interior) { // exterior after the probe: the lane without interior detectors
-        if (mixed_blocks_per_sm_ >= 3) return launch(k_lane_pass<float, 256, 3, 32, false>);
+        if (mixed_blocks_per_sm_ >= 4) return launch(k_lane_pass<float, 256, 4, 32, false>);
+        if (mixed_blocks_per_sm_ == 3) return launch(k_lane_pass<float, 256, 3, 32, false>);
         return launch(k_lane_pass<float, 256, 2, 32, false>);
     }
     if (mixed_blocks_per_sm_ >= 4) return launch(k_lane_pass<float, 256, 4>);

@@ -557,8 +557,8 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 // state then takes no registers.
 template <class T, bool INTR = true>
 MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
-                     int reflen, T ESC2f, int blamask, T& zrad_out, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip,
-                     unsigned long long& n_rebase, unsigned long long& n_exact, unsigned long long& n_ferebase) {
+                     int reflen, T ESC2f, int blamask, T& zrad_out, unsigned& n_steps, unsigned& n_bla, unsigned long long& n_skip,
+                     unsigned& n_rebase, unsigned& n_exact, unsigned& n_ferebase) {
     using R = LaneReal<T>;
     using Z = typename R::Z;
     const FrameGeom& g = p.g;
