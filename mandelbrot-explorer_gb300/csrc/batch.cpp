@@ -212,7 +212,10 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
     cudaMemsetAsync(d_ctr_, 0, 6 * sizeof(Counters), st_);
     cudaMemsetAsync(d_view_interior_, 0, sizeof(unsigned) * nviews, st_);
-    auto tiers = [&](const ViewDesc* views, unsigned total, int c0, unsigned* vint, const uint64_t* order) {
+    // probe_only: the probe's samples are rendered again by the main pass, so
+    // the probe needs only its FP32 tier (its gate counts unvouched interior
+    // decisions as interior)
+    auto tiers = [&](const ViewDesc* views, unsigned total, int c0, unsigned* vint, const uint64_t* order, bool probe_only) {
         BatchArgs a{};
         a.views = views;
         a.nviews = nviews;
@@ -226,6 +229,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.ctr = d_ctr_ + c0;
         a.next_queue = d_qa_;
         launch_batch_pass(0, a, nsm, st_);
+        if (probe_only) return;
         // double-float over the FP32 pass's queue
         a.queue = d_qa_;
         a.queue_n = &d_ctr_[c0].rerun_n;
@@ -239,15 +243,15 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.next_queue = nullptr;
         launch_batch_pass(2, a, nsm, st_);
     };
-    tiers(d_probe_, probe_total, 0, d_view_interior_, nullptr);
+    tiers(d_probe_, probe_total, 0, d_view_interior_, nullptr, true);
     launch_batch_gate(d_main_, nviews, d_view_interior_, st_);
     if (schedule_) {
         sched_probe_grid(d_probe_, d_main_, nviews, probe_total, st_);
         sched_order(sched_, d_main_, nviews, main_total, nsm, d_qo_, st_);
-        tiers(d_main_, main_total, 3, nullptr, d_qo_);
+        tiers(d_main_, main_total, 3, nullptr, d_qo_, false);
         if (schedule_ == 1) sched_train(sched_, d_main_, nviews, main_total, kSchedTrainSteps, 2e-3f, st_);
     } else {
-        tiers(d_main_, main_total, 3, nullptr, nullptr);
+        tiers(d_main_, main_total, 3, nullptr, nullptr, false);
     }
     cudaMemcpyAsync(h_ctr_, d_ctr_, 6 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
     e = cudaStreamEndCapture(st_, &graph_);
@@ -347,7 +351,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             return MBX_E_CANCELLED;
         }
         bs.pass_gpu_ms = ms;
-        bs.kernel_launches = 9; // per phase FP32, double-float (two widths), FP64; and the gate
+        bs.kernel_launches = 6; // probe FP32; gate; main FP32, double-float (two widths), FP64
         bs.passes = 2;
         for (int c = 0; c < 6; ++c) {
             const Counters& k = h_ctr_[c];
@@ -360,15 +364,16 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             bs.exact_steps += (long long)k.exact_steps;
             bs.fe_rebases += (long long)k.fe_rebases;
         }
-        bs.fp64_reruns = (long long)h_ctr_[0].rerun_n + h_ctr_[3].rerun_n;
-        bs.fp64_reruns_fp64 = (long long)h_ctr_[1].rerun_n + h_ctr_[4].rerun_n;
+        bs.fp64_reruns = (long long)h_ctr_[3].rerun_n; // the main pass's queues (the probe's are not rerun)
+        bs.fp64_reruns_fp64 = (long long)h_ctr_[4].rerun_n;
         bs.samples = (int)(probe_total + main_total);
         const unsigned want[2] = {probe_total, main_total};
         for (int ph = 0; ph < 2; ++ph) {
             const Counters* c = h_ctr_ + 3 * ph;
-            // every sample finishes in the FP32 pass or one of the queues it feeds
-            if (c[0].finished != want[ph] || c[1].finished != std::min(c[0].rerun_n, cap_samples_) ||
-                c[2].finished != std::min(c[1].rerun_n, cap_samples_)) {
+            // every sample finishes in the FP32 pass or one of the queues it
+            // feeds (the probe has no rerun tiers)
+            if (c[0].finished != want[ph] ||
+                (ph == 1 && (c[1].finished != std::min(c[0].rerun_n, cap_samples_) || c[2].finished != std::min(c[1].rerun_n, cap_samples_)))) {
                 err = "batched pass left samples unfinished";
                 return MBX_E_CUDA;
             }

@@ -1432,6 +1432,25 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     ++stats_.kernel_launches;
     if (e != cudaSuccess) return fail_cuda("mixed pass launch", e);
     cudaEventRecord(evm_, st_);
+    if (probe_gate_only_) {
+        // the interior gate's probe: its samples are rendered again by the
+        // main pass, so its queue is not rerun; its gate counts the interior
+        // decisions the FP32 lane could not vouch for as interior
+        cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+        e = cudaStreamSynchronize(st_);
+        stats_.kernel_ms += now_ms() - t0;
+        if (e != cudaSuccess) return fail_cuda("mixed probe pass", e);
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev0_, evm_) == cudaSuccess) stats_.pass_gpu_ms += ms;
+        if (cancel_.load()) return MBX_E_CANCELLED;
+        hctr_->interior += hctr_->interior_flagged;
+        stats_.steps += (long long)hctr_->steps;
+        stats_.bla_applies += (long long)hctr_->bla_applies;
+        stats_.bla_skipped += (long long)hctr_->bla_skipped;
+        stats_.samples += n;
+        if ((int)hctr_->finished < n) hctr_->interior += 1; // samples left unstarted: keep the detectors on
+        return MBX_OK;
+    }
     auto queue_frame = [&](uint64_t* q, int ctr_in, uint64_t* next_q, int ctr_out) {
         DeviceFrame r = frame_view();
         r.px = PixelSet();
@@ -1981,7 +2000,9 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
         g.skip_i = g.skip_j = -1;
         g.n = ((H_ + 7) / 8) * ((W_ + 7) / 8);
         grid_pending_.clear();
+        probe_gate_only_ = true;
         rc = run_pass(nullptr, g, ref_it, nullptr, nullptr);
+        probe_gate_only_ = false;
         if (rc != MBX_OK) return rc;
         if (hctr_->interior == 0) use_interior_ = false;
     }

@@ -225,6 +225,7 @@ class Engine {
     std::vector<double> hdpxy_;
     std::vector<float> hdpxyf_;
     int dpxy_w_ = 0;
+    bool probe_gate_only_ = false; // mixed form: the gate's probe pass runs its FP32 tier only
     DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
     DevBuf<uint64_t> drerun2_keys_;           // double-float pass: queue for the FP64 pass
     DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position

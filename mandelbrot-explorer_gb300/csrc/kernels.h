@@ -116,6 +116,7 @@ struct Counters {
     unsigned int rerun_n;                // mixed pass: entries queued for the FP64 floatexp pass
     unsigned int finished;               // mixed pass: entries finished or queued
     unsigned int gmp_flags;              // floatexp pass: entries flagged for the arbitrary-precision recompute
+    unsigned int interior_flagged;       // lane passes: interior decisions queued for the next tier
     unsigned long long exact_steps;      // lane passes: steps taken in FP64 floatexp (orbit or delta below the lane's range)
     unsigned long long fe_rebases;       // lane passes: rebases decided in FP64 floatexp
 };

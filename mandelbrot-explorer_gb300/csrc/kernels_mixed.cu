@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     const unsigned lane_id = threadIdx.x & 31;
     // per-thread counts of one pass (32-bit: a thread executes far fewer than
     // 2^32 steps per pass); skipped and effective iterations stay 64-bit
-    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0, n_intflag = 0;
     unsigned long long n_skip = 0, n_eff = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
@@ -154,7 +154,8 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
                 n_eff += (unsigned long long)g.mxit;
                 ++n_int;
                 live = false;
-            } else if (LaneReal<T>::kTrackError && st == 3) { // queued for the FP64 pass that follows
+            } else if (LaneReal<T>::kTrackError && st >= 3) { // queued for the next tier
+                if (st == 4) ++n_intflag;
                 int a[4];
                 entry_coords(f.px, L.i, a);
                 const unsigned q = atomicAdd(&f.ctr->rerun_n, 1u);
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     atomicAdd(&f.ctr->exact_steps, (unsigned long long)n_exact);
     atomicAdd(&f.ctr->fe_rebases, (unsigned long long)n_ferebase);
     atomicAdd(&f.ctr->finished, n_fin);
+    if (n_intflag) atomicAdd(&f.ctr->interior_flagged, n_intflag);
     atomicAdd(&f.ctr->interior, n_int);
 }
 
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     const unsigned lane_id = threadIdx.x & 31;
     // per-thread counts of one pass (32-bit: a thread executes far fewer than
     // 2^32 steps per pass); skipped and effective iterations stay 64-bit
-    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0;
+    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0, n_intflag = 0;
     unsigned long long n_skip = 0, n_eff = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
@@ -284,7 +286,9 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
                 n_eff += (unsigned long long)vd.p.g.mxit;
                 ++n_int;
                 live = false;
-            } else if (LaneReal<T>::kTrackError && st == 3) {
+            } else if (LaneReal<T>::kTrackError && st >= 3) {
+                // an unvouched interior decision counts for the probe's gate
+                if (st == 4 && a.view_interior) atomicAdd(&a.view_interior[view], 1u);
                 int c[4];
                 const int row = (L.oidx / (vd.p.g.W * vd.p.g.sub)), col = L.oidx % (vd.p.g.W * vd.p.g.sub);
                 c[0] = row / vd.p.g.sub;

@@ -541,17 +541,18 @@ MBX_HD void lane_z_double(const Lane<T>& L, const double2* Zd, double& zr, doubl
     zi = Xd.y + sd * (double)L.wi;
 }
 
-// Interior decision: an FP32 lane whose error estimate is too large leaves
-// for the FP64 pass (3) instead of reporting interior (2).
+// Interior decision: a lane whose error estimate is too large leaves for the
+// next tier (4: an interior decision it cannot vouch for) instead of reporting
+// interior (2).
 template <class T>
 MBX_HD int lane_interior(const Lane<T>& L) {
-    if (LaneReal<T>::kTrackError && lane_rel_err2(L.err2, L.wr, L.wi) > kLaneInteriorTol2) return 3;
+    if (LaneReal<T>::kTrackError && lane_rel_err2(L.err2, L.wr, L.wi) > kLaneInteriorTol2) return 4;
     return 2;
 }
 
 // Advance one lane by up to `budget` iterations. Returns 0 running, 1 escaped,
-// 2 interior, 3 precision spent (FP32 lane only: rerun in FP64); zrad_out is
-// set on escape.
+// 2 interior, 3 precision spent and 4 an unvouched interior decision (lanes
+// with an error estimate: rerun in the next tier); zrad_out is set on escape.
 // INTR = false compiles the lane without its interior detectors, for passes
 // whose interior detection is off (exterior frames after the probe): their
 // state then takes no registers.
