@@ -255,7 +255,7 @@ def main():
             bla += st["bla_applies"]
             launches += st["kernel_launches"]
             gpu_ms += st["pass_gpu_ms"]
-            reruns[v["label"]] = st["fp64_reruns"]
+            reruns[v["label"]] = {"double_float": st["fp64_reruns"], "exact_form": st["exact_reruns"]}
         return eff, steps, bla, launches, gpu_ms, per_view
 
     # warm-up (the first step builds each frame's reference)
@@ -445,7 +445,7 @@ def main():
                 "autotuned": tuning,
                 "batched": batched,
                 "image_epilogue": epilogue,
-                "fp64_reruns_per_frame": reruns,
+                "reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_batch_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": eb_t / 2 * 1e3,
                     "api": "mbx_compute_batch (both frames per call, host buffers, fresh GMP references)",

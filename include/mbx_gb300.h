@@ -86,10 +86,11 @@ typedef struct {
     long long rebases;              /* rebases taken (mixed form) */
     long long fp64_reruns;          /* mixed form: samples rerun in double-float (FP32 error estimate too large) */
     double rerun_gpu_ms;            /* device time of the reruns (included in pass_gpu_ms) */
-    long long fp64_reruns_fp64;     /* of those, samples rerun again in FP64 (double-float estimate too large) */
-    double rerun_fp64_gpu_ms;       /* device time of the FP64 reruns (included in rerun_gpu_ms) */
-    long long exact_steps;          /* mixed form: steps taken in FP64 floatexp (orbit or delta below FP32's range) */
-    long long fe_rebases;           /* mixed form: rebases decided in FP64 floatexp (inside the margin, end of reference) */
+    long long fp64_reruns_fp64;     /* of those, samples rerun again in FP64: the exact form (double-float estimate too large) */
+    double rerun_fp64_gpu_ms;       /* device time of the exact-form reruns (included in rerun_gpu_ms) */
+    long long exact_steps;          /* mixed form: steps taken in floatexp (orbit or delta below the lane type's range) */
+    long long fe_rebases;           /* mixed form: rebases decided in floatexp (inside the margin, end of reference) */
+    long long exact_reruns;         /* mixed form: samples finished by the exact form (no tier could vouch for them; equals fp64_reruns_fp64) */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns
@@ -116,7 +117,7 @@ typedef struct {
     int threads;            /* block size: 128 or 256 */
     int blocks_per_sm;      /* resident blocks per SM the kernel is compiled for: 2, 3 or 4 */
     int smem_orbit_limit;   /* stage the FP32 orbit into shared memory when it fits in this many bytes (0: never) */
-    double rescale_window;  /* |w|^2 is kept in [1/window, window] */
+    double rescale_window;  /* |w|^2 is kept in [1/window, window]; 1e4 to 1e16 */
     double pass_ms;         /* autotune: GPU time of the calibration pass with this shape */
 } mbx_tuning;
 

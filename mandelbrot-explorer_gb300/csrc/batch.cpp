@@ -82,7 +82,7 @@ int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err)
         g_views_ = -1; // the graph holds the old pointers
     }
     if (!d_ctr_) {
-        if (cudaMalloc(&d_ctr_, 6 * sizeof(Counters)) != cudaSuccess || cudaHostAlloc((void**)&h_ctr_, 6 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) {
+        if (cudaMalloc(&d_ctr_, 4 * sizeof(Counters)) != cudaSuccess || cudaHostAlloc((void**)&h_ctr_, 4 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) {
             err = "batch counter allocation failed";
             return MBX_E_NOMEM;
         }
@@ -210,7 +210,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     int nsm = eng_[0]->sm_count();
     cudaError_t e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
-    cudaMemsetAsync(d_ctr_, 0, 6 * sizeof(Counters), st_);
+    cudaMemsetAsync(d_ctr_, 0, 4 * sizeof(Counters), st_);
     cudaMemsetAsync(d_view_interior_, 0, sizeof(unsigned) * nviews, st_);
     // probe_only: the probe's samples are rendered again by the main pass, so
     // the probe needs only its FP32 tier (its gate counts unvouched interior
@@ -230,30 +230,25 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.next_queue = d_qa_;
         launch_batch_pass(0, a, nsm, st_);
         if (probe_only) return;
-        // double-float over the FP32 pass's queue
+        // double-float over the FP32 pass's queue; what it cannot vouch for
+        // is queued for the views' exact form (host side, after the graph)
         a.queue = d_qa_;
         a.queue_n = &d_ctr_[c0].rerun_n;
         a.ctr = d_ctr_ + c0 + 1;
         a.next_queue = d_qb_;
         launch_batch_pass(1, a, nsm, st_);
-        // FP64 over the double-float pass's queue
-        a.queue = d_qb_;
-        a.queue_n = &d_ctr_[c0 + 1].rerun_n;
-        a.ctr = d_ctr_ + c0 + 2;
-        a.next_queue = nullptr;
-        launch_batch_pass(2, a, nsm, st_);
     };
     tiers(d_probe_, probe_total, 0, d_view_interior_, nullptr, true);
     launch_batch_gate(d_main_, nviews, d_view_interior_, st_);
     if (schedule_) {
         sched_probe_grid(d_probe_, d_main_, nviews, probe_total, st_);
         sched_order(sched_, d_main_, nviews, main_total, nsm, d_qo_, st_);
-        tiers(d_main_, main_total, 3, nullptr, d_qo_, false);
+        tiers(d_main_, main_total, 2, nullptr, d_qo_, false);
         if (schedule_ == 1) sched_train(sched_, d_main_, nviews, main_total, kSchedTrainSteps, 2e-3f, st_);
     } else {
-        tiers(d_main_, main_total, 3, nullptr, nullptr, false);
+        tiers(d_main_, main_total, 2, nullptr, nullptr, false);
     }
-    cudaMemcpyAsync(h_ctr_, d_ctr_, 6 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(h_ctr_, d_ctr_, 4 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
     e = cudaStreamEndCapture(st_, &graph_);
     if (e != cudaSuccess) return cuda_fail(err, "graph capture", e);
     e = cudaGraphInstantiate(&exec_, graph_, 0);
@@ -351,9 +346,9 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             return MBX_E_CANCELLED;
         }
         bs.pass_gpu_ms = ms;
-        bs.kernel_launches = 6; // probe FP32; gate; main FP32, double-float (two widths), FP64
+        bs.kernel_launches = 5; // probe FP32; gate; main FP32, double-float (two widths)
         bs.passes = 2;
-        for (int c = 0; c < 6; ++c) {
+        for (int c = 0; c < 4; ++c) {
             const Counters& k = h_ctr_[c];
             bs.steps += (long long)k.steps;
             bs.bla_applies += (long long)k.bla_applies;
@@ -364,18 +359,47 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             bs.exact_steps += (long long)k.exact_steps;
             bs.fe_rebases += (long long)k.fe_rebases;
         }
-        bs.fp64_reruns = (long long)h_ctr_[3].rerun_n; // the main pass's queues (the probe's are not rerun)
-        bs.fp64_reruns_fp64 = (long long)h_ctr_[4].rerun_n;
+        bs.fp64_reruns = (long long)h_ctr_[2].rerun_n; // the main pass's queues (the probe's are not rerun)
+        bs.fp64_reruns_fp64 = (long long)h_ctr_[3].rerun_n;
         bs.samples = (int)(probe_total + main_total);
         const unsigned want[2] = {probe_total, main_total};
         for (int ph = 0; ph < 2; ++ph) {
-            const Counters* c = h_ctr_ + 3 * ph;
+            const Counters* c = h_ctr_ + 2 * ph;
             // every sample finishes in the FP32 pass or one of the queues it
             // feeds (the probe has no rerun tiers)
-            if (c[0].finished != want[ph] ||
-                (ph == 1 && (c[1].finished != std::min(c[0].rerun_n, cap_samples_) || c[2].finished != std::min(c[1].rerun_n, cap_samples_)))) {
+            if (c[0].finished != want[ph] || (ph == 1 && c[1].finished != std::min(c[0].rerun_n, cap_samples_))) {
                 err = "batched pass left samples unfinished";
                 return MBX_E_CUDA;
+            }
+        }
+        // samples the double-float tier could not vouch for: each view's exact
+        // form finishes its own (keys carry the view's position among the deferred)
+        const unsigned n_exact = std::min(h_ctr_[3].rerun_n, cap_samples_);
+        bs.exact_reruns = (long long)n_exact;
+        if (n_exact > 0) {
+            std::vector<uint64_t> q(n_exact);
+            cudaMemcpyAsync(q.data(), d_qb_, sizeof(uint64_t) * n_exact, cudaMemcpyDeviceToHost, st_);
+            e = cudaStreamSynchronize(st_);
+            if (e != cudaSuccess) return cuda_fail(err, "double-float rerun readback", e);
+            std::vector<unsigned> vint((size_t)nv);
+            cudaMemcpyAsync(vint.data(), d_view_interior_, sizeof(unsigned) * nv, cudaMemcpyDeviceToHost, st_);
+            e = cudaStreamSynchronize(st_);
+            if (e != cudaSuccess) return cuda_fail(err, "interior gate readback", e);
+            std::vector<std::vector<uint64_t>> per((size_t)nv);
+            for (uint64_t k : q) {
+                const int v = (int)(k >> kBatchViewShift);
+                if (v < 0 || v >= nv) {
+                    err = "batched rerun queue holds a bad view index";
+                    return MBX_E_CUDA;
+                }
+                per[(size_t)v].push_back(k & ((1ull << kBatchViewShift) - 1ull));
+            }
+            for (int k = 0; k < nv; ++k) {
+                rc = eng_[deferred[k]]->batch_exact_rerun(per[(size_t)k], vint[(size_t)k] > 0);
+                if (rc != MBX_OK) {
+                    err = eng_[deferred[k]]->error();
+                    return rc;
+                }
             }
         }
         for (int k = 0; k < nv; ++k) {

@@ -40,11 +40,11 @@ class BatchRunner {
     ViewDesc* d_probe_ = nullptr;
     ViewDesc* d_main_ = nullptr;
     ViewDesc* h_desc_ = nullptr;   // pinned staging: probe descriptors then main descriptors
-    Counters* d_ctr_ = nullptr;    // 6 blocks: probe FP32 / double-float / FP64, main likewise
+    Counters* d_ctr_ = nullptr;    // 4 blocks: probe FP32 / double-float, main likewise
     Counters* h_ctr_ = nullptr;
     unsigned* d_view_interior_ = nullptr;
     uint64_t* d_qa_ = nullptr;     // FP32 -> double-float queue
-    uint64_t* d_qb_ = nullptr;     // double-float -> FP64 queue
+    uint64_t* d_qb_ = nullptr;     // double-float -> the views' exact form
     int cap_views_ = 0;
     unsigned cap_samples_ = 0;
     cudaGraph_t graph_ = nullptr;

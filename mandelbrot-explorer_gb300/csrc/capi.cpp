@@ -221,7 +221,7 @@ int mbx_autotune(mbx_context* c, const mbx_request* calib, mbx_tuning* best) {
     const int threads_opts[] = {128, 256};
     const int blocks_opts[] = {2, 3, 4};
     const int smem_opts[] = {200 * 1024, 0};
-    const double window_opts[] = {1e8, 1e16, 1e30};
+    const double window_opts[] = {1e8, 1e12, 1e16};
     double best_ms = 1e300;
     mbx_tuning b = {};
     for (int t : threads_opts)

@@ -259,12 +259,10 @@ int Engine::init(std::string& err) {
     nsm_ = prop.multiProcessorCount;
     snprintf(devname_, sizeof(devname_), "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor, nsm_);
     if (cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess) return -1;
-    // Counters of a pass, and of the two rerun passes that follow a mixed pass.
-    if (cudaMalloc(&dctr_, 3 * sizeof(Counters)) != cudaSuccess) return -1;
-    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess || cudaEventCreate(&evm_) != cudaSuccess ||
-        cudaEventCreate(&evd_) != cudaSuccess)
-        return -1;
-    if (cudaHostAlloc(&hctr_, 3 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) return -1;
+    // Counters of a pass, and of the double-float rerun pass that follows a mixed pass.
+    if (cudaMalloc(&dctr_, 2 * sizeof(Counters)) != cudaSuccess) return -1;
+    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess || cudaEventCreate(&evm_) != cudaSuccess) return -1;
+    if (cudaHostAlloc(&hctr_, 2 * sizeof(Counters), cudaHostAllocDefault) != cudaSuccess) return -1;
     if (cudaHostAlloc((void**)&hcancel_, sizeof(int), cudaHostAllocMapped) != cudaSuccess) return -1;
     *hcancel_ = 0;
     if (cudaHostGetDevicePointer((void**)&dcancel_, (void*)hcancel_, 0) != cudaSuccess) return -1;
@@ -275,7 +273,7 @@ void Engine::release_device() {
     if (st_) cudaStreamSynchronize(st_);
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
-                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dbla64_.p,
+                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dbla32_.p,
                     (void*)drerun_keys_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p,
                     (void*)dcost_.p, (void*)dpgrid_.p, (void*)ddpxy_.p, (void*)ddpxyf_.p})
         if (p) cudaFree(p);
@@ -283,7 +281,6 @@ void Engine::release_device() {
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (evm_) cudaEventDestroy(evm_);
-    if (evd_) cudaEventDestroy(evd_);
     if (hctr_) cudaFreeHost(hctr_);
     if (hcancel_) cudaFreeHost((void*)hcancel_);
     if (st_) cudaStreamDestroy(st_);
@@ -1421,7 +1418,7 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     if (!ensure(ddone_, n) || !ensure(drerun_keys_, n) || !ensure(drerun2_keys_, n) || !ensure(drerun_done_, n) || !ensure(drerun_gmp_, n))
         return MBX_E_NOMEM;
     cudaMemsetAsync(ddone_.p, 0, n, st_);
-    cudaMemsetAsync(dctr_, 0, 3 * sizeof(Counters), st_);
+    cudaMemsetAsync(dctr_, 0, 2 * sizeof(Counters), st_);
     ++stats_.passes;
     DeviceFrame f = frame_view();
     f.px = px;
@@ -1468,24 +1465,19 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     e = run_df_pass(queue_frame(drerun_keys_.p, 0, drerun2_keys_.p, 1));
     stats_.kernel_launches += 2; // narrow and wide variants, one of which runs
     if (e != cudaSuccess) return fail_cuda("double-float rerun launch", e);
-    cudaEventRecord(evd_, st_);
-    e = run_rerun_pass(queue_frame(drerun2_keys_.p, 1, nullptr, 2));
-    ++stats_.kernel_launches;
-    if (e != cudaSuccess) return fail_cuda("FP64 rerun launch", e);
     cudaEventRecord(ev1_, st_);
-    cudaMemcpyAsync(hctr_, dctr_, 3 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(hctr_, dctr_, 2 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("mixed pass", e);
     {
-        float ms = 0.0f, rms = 0.0f, fms = 0.0f;
+        float ms = 0.0f, rms = 0.0f;
         if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) stats_.pass_gpu_ms += ms;
         if (cudaEventElapsedTime(&rms, evm_, ev1_) == cudaSuccess) stats_.rerun_gpu_ms += rms;
-        if (cudaEventElapsedTime(&fms, evd_, ev1_) == cudaSuccess) stats_.rerun_fp64_gpu_ms += fms;
     }
     if (cancel_.load()) return MBX_E_CANCELLED;
     Counters& a = hctr_[0];
-    for (int k = 1; k < 3; ++k) {
+    for (int k = 1; k < 2; ++k) {
         const Counters& b = hctr_[k];
         a.steps += b.steps;
         a.bla_applies += b.bla_applies;
@@ -1504,7 +1496,9 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     stats_.fp64_reruns += std::min<unsigned>(a.rerun_n, (unsigned)n);
     stats_.fp64_reruns_fp64 += std::min<unsigned>(hctr_[1].rerun_n, (unsigned)n);
     stats_.samples += n;
-    if ((int)a.finished < n) {
+    const bool unstarted = (int)a.finished < n;
+    const unsigned n_exact = std::min<unsigned>(hctr_[1].rerun_n, (unsigned)n);
+    if (unstarted) {
         // A block left samples unstarted (orbit staging timed out): scan the
         // flags and take them through the FP64 floatexp pass.
         hdone_.resize(n);
@@ -1526,6 +1520,30 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         g.skip_i = g.skip_j = -1;
         const int rc = run_pass(&pending, g, mx_ref_it, nullptr, nullptr);
         exact_rerun_ = false;
+        if (rc != MBX_OK) return rc;
+        if (!pending.empty()) {
+            err_ = "floatexp pass left samples unfinished";
+            return MBX_E_CUDA;
+        }
+    }
+    if (n_exact > 0) {
+        // Samples the double-float estimate cannot vouch for either: the exact
+        // form (the reference's FP64 floatexp loop with its arbitrary-precision
+        // recomputes) finishes them, so every sample carries either a vouched
+        // result or the exact form's.
+        std::vector<uint64_t> pending(n_exact);
+        cudaMemcpyAsync(pending.data(), drerun2_keys_.p, sizeof(uint64_t) * n_exact, cudaMemcpyDeviceToHost, st_);
+        e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return fail_cuda("double-float rerun readback", e);
+        stats_.exact_reruns += (long long)n_exact;
+        const double gpu0 = stats_.pass_gpu_ms;
+        exact_rerun_ = true;
+        PixelSet g = PixelSet();
+        g.grid_w = g.grid_h = g.grid_step = 1;
+        g.skip_i = g.skip_j = -1;
+        const int rc = run_pass(&pending, g, mx_ref_it, nullptr, nullptr);
+        exact_rerun_ = false;
+        stats_.rerun_fp64_gpu_ms += stats_.pass_gpu_ms - gpu0;
         if (rc != MBX_OK) return rc;
         if (!pending.empty()) {
             err_ = "floatexp pass left samples unfinished";
@@ -1744,8 +1762,6 @@ void Engine::fill_batch_slot() {
     d.orb32 = dZf_.p;
     d.bladf = dbladf_.p;
     d.orbdf = dZdf_.p;
-    d.bla64 = dbla64_.p;
-    d.orb64 = dZ_.p;
     d.interior_gate = 0;
     d.base = 0;
     // probe on the 1/8 grid with interior detection on (mp.cpp:1668-1720)
@@ -1793,6 +1809,28 @@ int Engine::compute_deferred(const mbx_request& r, BatchSlot* slot, mbx_stats* o
     const int rc = compute(r, out_stats);
     batch_slot_ = nullptr;
     return rc;
+}
+
+int Engine::batch_exact_rerun(std::vector<uint64_t>& keys, bool interior_seen) {
+    if (keys.empty()) return MBX_OK;
+    stats_.exact_reruns += (long long)keys.size();
+    stats_.fp64_reruns_fp64 += (long long)keys.size();
+    // interior detection as the single-frame render's gate leaves it
+    const bool interior = use_interior_;
+    if (!interior_seen) use_interior_ = false;
+    exact_rerun_ = true;
+    PixelSet g = PixelSet();
+    g.grid_w = g.grid_h = g.grid_step = 1;
+    g.skip_i = g.skip_j = -1;
+    const int rc = run_pass(&keys, g, batch_ref_it_, nullptr, nullptr);
+    exact_rerun_ = false;
+    use_interior_ = interior;
+    if (rc != MBX_OK) return rc;
+    if (!keys.empty()) {
+        err_ = "floatexp pass left samples unfinished";
+        return MBX_E_CUDA;
+    }
+    return MBX_OK;
 }
 
 int Engine::batch_finish(const mbx_request& r, mbx_stats* out_stats) {
@@ -1987,6 +2025,7 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     if (rc != MBX_OK) return rc;
     if (progress) *progress = 0.08f;
     if (batch_slot_ && use_floatexp_ && mixed_active() && SUB_ == 1) {
+        batch_ref_it_ = ref_it;
         fill_batch_slot(); // the probe and main passes run in the batch's launches
         return MBX_OK;
     }

@@ -93,6 +93,10 @@ class Engine {
     // finish copies host outputs and completes the stats of a deferred frame.
     int compute_deferred(const mbx_request& r, BatchSlot* slot, mbx_stats* st);
     int batch_finish(const mbx_request& r, mbx_stats* st);
+    // the exact form over a deferred frame's samples the batched tiers could
+    // not vouch for (keys as key_pack; emptied on success); interior_seen: the
+    // batch's interior gate found interior samples in this frame's probe
+    int batch_exact_rerun(std::vector<uint64_t>& keys, bool interior_seen);
     cudaStream_t stream() const { return st_; }
     volatile int* device_cancel_flag() const { return dcancel_; }
     int sm_count() const { return nsm_; }
@@ -110,7 +114,6 @@ class Engine {
     int run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_ref_it);
     FeParams fe_params(int mx_ref_it) const;
     cudaError_t run_mixed_pass(const DeviceFrame& f);
-    cudaError_t run_rerun_pass(const DeviceFrame& f);
     cudaError_t run_df_pass(const DeviceFrame& f);
     MixedParams mixed_params() const;
     int prepare_mixed();
@@ -215,7 +218,6 @@ class Engine {
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
     DevBuf<Bla32> dbla32_;
-    DevBuf<Bla64> dbla64_;
     DevBuf<BlaDF> dbladf_;
     DevBuf<df2> dZdf_;
     DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample lane cost
@@ -227,18 +229,25 @@ class Engine {
     int dpxy_w_ = 0;
     bool probe_gate_only_ = false; // mixed form: the gate's probe pass runs its FP32 tier only
     DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
-    DevBuf<uint64_t> drerun2_keys_;           // double-float pass: queue for the FP64 pass
+    DevBuf<uint64_t> drerun2_keys_;           // double-float pass: samples it cannot vouch for (the exact form finishes them)
     DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position
     bool exact_rerun_ = false; // mixed form: the FP64 floatexp rerun of flagged samples is running
     BatchSlot* batch_slot_ = nullptr;
     void fill_batch_slot();
+    int batch_ref_it_ = 0; // reference length of the deferred frame's passes
     // The FP32 pass carries no derivative: DE colourings take the exact form.
     bool mixed_active() const { return mode_ == MBX_PRECISION_MIXED && !deriv_; }
 
-    // mixed-pass launch shape (set by the autotuner / defaults)
+    // mixed-pass launch shape (set by the autotuner / defaults: orbit read
+    // through L1, the choice of the autotuner on both 1080p deep frames).
+    // The rescale window |w|^2 in [1/wmax2, wmax2] stays at or below 1e16:
+    // with a wider one, |w| down to 1e-15 times an orbit value near the
+    // lanes' 1e-30 floor leaves FP32's normal range (and the double-float
+    // low parts leave it 2^24 sooner), a rounding loss the error estimate
+    // does not model (class errors on a 1e-875 minibrot frame at 1e30).
     int mixed_threads_ = 256;
     int mixed_blocks_per_sm_ = 3;
-    int smem_orbit_limit_ = 200 * 1024;
+    int smem_orbit_limit_ = 0;
     float mixed_wmax2_ = 1e16f;
 
   public:
@@ -246,7 +255,7 @@ class Engine {
         if (threads == 128 || threads == 256) mixed_threads_ = threads;
         if (blocks_per_sm >= 1 && blocks_per_sm <= 4) mixed_blocks_per_sm_ = blocks_per_sm;
         if (smem_limit >= 0 && smem_limit <= 220 * 1024) smem_orbit_limit_ = smem_limit;
-        if (wmax2 >= 1e4f && wmax2 <= 1e30f) mixed_wmax2_ = wmax2;
+        if (wmax2 >= 1e4f && wmax2 <= 1e16f) mixed_wmax2_ = wmax2;
     }
     void get_tuning(int* threads, int* blocks_per_sm, int* smem_limit, float* wmax2) const {
         *threads = mixed_threads_;
@@ -276,7 +285,7 @@ class Engine {
     std::string frame_key_;
     bool reuse_ = false;
     int refs_built_in_frame_ = 0;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evm_ = nullptr, evd_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evm_ = nullptr;
     void save_cache(int ref_it);
     bool restore_cache(int* ref_it);
 

@@ -117,8 +117,8 @@ struct Counters {
     unsigned int finished;               // mixed pass: entries finished or queued
     unsigned int gmp_flags;              // floatexp pass: entries flagged for the arbitrary-precision recompute
     unsigned int interior_flagged;       // lane passes: interior decisions queued for the next tier
-    unsigned long long exact_steps;      // lane passes: steps taken in FP64 floatexp (orbit or delta below the lane's range)
-    unsigned long long fe_rebases;       // lane passes: rebases decided in FP64 floatexp
+    unsigned long long exact_steps;      // lane passes: steps taken in floatexp (orbit or delta below the lane's range)
+    unsigned long long fe_rebases;       // lane passes: rebases decided in floatexp
 };
 
 struct FrameGeom {
@@ -224,8 +224,8 @@ struct MixedParams {
                              // variant runs when the queue holds >= wide_from
                              // entries, the narrow one below (0: no selection)
 };
-// The lane passes are launched by Engine::run_mixed_pass / run_df_pass /
-// run_rerun_pass (kernels_mixed.cu), which own their per-reference tables.
+// The lane passes are launched by Engine::run_mixed_pass / run_df_pass
+// (kernels_mixed.cu), which own their per-reference tables.
 
 // One view of a batch: what a lane needs to iterate that view's samples. The
 // batch passes read it from device memory per lane, so lanes of one warp may
@@ -237,8 +237,6 @@ struct ViewDesc {
     const float2* orb32;
     const BlaDF* bladf;
     const df2* orbdf;
-    const Bla64* bla64;
-    const double2* orb64;
     unsigned base;           // first batch-wide sample index of this view
     unsigned count;          // samples of this view in the pass
     int interior_gate;       // main pass: interior detection follows the probe's interior count

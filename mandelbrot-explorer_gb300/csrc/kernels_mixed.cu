@@ -196,11 +196,6 @@ struct ViewTables<df32> {
     __device__ static const BlaDF* bla(const ViewDesc& v) { return v.bladf; }
     __device__ static const df2* orb(const ViewDesc& v) { return v.orbdf; }
 };
-template <>
-struct ViewTables<double> {
-    __device__ static const Bla64* bla(const ViewDesc& v) { return v.bla64; }
-    __device__ static const double2* orb(const ViewDesc& v) { return v.orb64; }
-};
 
 // One persistent launch over the samples of several views: the FP32 pass takes
 // all views' pixel sets back to back (a batch-wide work counter, so SMs that
@@ -407,11 +402,10 @@ int Engine::prepare_mixed() {
     stats_.kernel_launches += 2;
     if (bla_.use && bla_.nlev > 0) {
         int n = bla_.off[bla_.nlev - 1] + bla_.size[bla_.nlev - 1];
-        if (!ensure(dbla32_, (size_t)n) || !ensure(dbladf_, (size_t)n) || !ensure(dbla64_, (size_t)n)) return MBX_E_NOMEM;
+        if (!ensure(dbla32_, (size_t)n) || !ensure(dbladf_, (size_t)n)) return MBX_E_NOMEM;
         k_bla_to_lane<float><<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbla32_.p, n);
         k_bla_to_lane<df32><<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbladf_.p, n);
-        k_bla_to_lane<double><<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbla64_.p, n);
-        stats_.kernel_launches += 3;
+        stats_.kernel_launches += 2;
     }
     return cuda_ok("mixed preparation");
 }
@@ -496,28 +490,16 @@ cudaError_t Engine::run_df_pass(const DeviceFrame& f) {
     return cudaGetLastError();
 }
 
-// The FP64 lane pass over the double-float pass's queue (entry count on the device).
-cudaError_t Engine::run_rerun_pass(const DeviceFrame& f) {
-    const MixedParams p = mixed_params();
-    DeviceFrame g = f;
-    if (!(bla_.use && dbla64_.p)) g.bla.use = 0;
-    const int threads = 128;
-    const int blocks = std::max(1, std::min((f.px.n + 31) / 32, nsm_ * 4));
-    k_lane_pass<double, 128, 2, 8><<<blocks, threads, 0, st_>>>(g, p, dbla64_.p, dZ_.p);
-    return cudaGetLastError();
-}
-
-// Batched passes (one FP32 launch over all views, then the two rerun tiers).
+// Batched passes: one FP32 launch over all views, then the double-float tier
+// (what it cannot vouch for goes to each view's exact form on the host side).
 cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st) {
     if (tier == 0) {
         k_batch_pass<float, 256, 3><<<nsm * 3, 256, 0, st>>>(a);
-    } else if (tier == 1) {
+    } else {
         BatchArgs b = a;
         b.wide_from = kWideLanesPerSm * (unsigned)nsm;
         k_batch_pass<df32, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(b);
         k_batch_pass<df32, 128, 2, 32><<<nsm * 4, 128, 0, st>>>(b);
-    } else {
-        k_batch_pass<double, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(a);
     }
     return cudaGetLastError();
 }

@@ -4,12 +4,14 @@
 //
 // Two instantiations run on the device (kernels_mixed.cu):
 //   * T = float: the mixed-precision pass. A running error estimate decides
-//     which FP32 results it may keep; it queues the other samples for
-//   * T = double: the FP64 rerun pass, the same lane in double precision, which
-//     costs ~15 FP64 operations per step (the reference-exact floatexp kernel
-//     spends several times that on floatexp bookkeeping).
-// Host-and-device code: the same source compiles as plain C++ so a host build
-// can step one sample for inspection. Semantics follow the reference's
+//     which FP32 results it may keep; it queues the other samples for the
+//     double-float tier.
+//   * T = df32: that tier, the same lane in double-float on the FP32 pipe; what
+//     its own estimate cannot vouch for goes to the exact form (the
+//     reference's FP64 floatexp loop, kernels_exact.cu).
+// T = double compiles as well (the lane in FP64 with its own estimate), for
+// host builds. Host-and-device code: the same source compiles as plain C++ so
+// a host build can step one sample for inspection. Semantics follow the reference's
 // rescaled loop (src/engine/mandel_perturbation.cpp:3287-3618, "mp.cpp").
 #pragma once
 #include <math.h>
@@ -150,15 +152,20 @@ template <>
 struct LaneReal<float> {
     using V2 = float2;
     static constexpr float kTinyX = 1e-30f;         // orbit entries below: exact floatexp step
-    static constexpr float kMinS = 7.888609e-31f;  // 2^-100: first step after a rebase needs s above this
+    static constexpr float kMinS = 8.881784e-16f;  // 2^-50: first step after a rebase needs s above this (|w'| ~ s stays normal)
+    static constexpr float kWFloor = 1e-30f;       // |w|^2 floor of the error estimate (err2 ~ 2^-47 |w|^2 stays normal)
     static constexpr float kEscLo = 0.999998f;     // escape screen margins around R^2
     static constexpr float kEscHi = 1.000002f;
     static constexpr int kExpClamp = 120;
     static constexpr bool kTrackError = true;
-    static constexpr float kEps2 = 7.105427e-15f; // 2 * (2^-24)^2: per-step rounding variance
+    using E = float;                              // the error estimate's type
+    static constexpr E kEps2 = 7.105427e-15f;     // 2 * (2^-24)^2: per-step rounding variance
+    static constexpr E kErrMax = 3e38f;           // saturation of the estimate
+    static constexpr int kRatioClamp = 300;       // exponent clamp of (S_old / S_new)^2
     using Z = float;                              // screens (|z|^2, |w|^2 and the like)
     MBX_HD static V2 make2(float a, float b) { return make_float2(a, b); }
     MBX_HD static float tof(float x) { return x; }
+    MBX_HD static float toe(float x) { return x; }
     MBX_HD static float z(float x) { return x; }
     MBX_HD static float zabs2(float a, float b) { return a * a + b * b; }
 };
@@ -167,14 +174,21 @@ struct LaneReal<double> {
     using V2 = double2;
     static constexpr double kTinyX = 1e-290;
     static constexpr double kMinS = 9.332636185032189e-302; // 2^-1000
+    static constexpr double kWFloor = 1e-290;
     static constexpr double kEscLo = 1.0;
     static constexpr double kEscHi = 1.0;
     static constexpr int kExpClamp = 1000;
-    static constexpr bool kTrackError = false;
-    static constexpr float kEps2 = 0.0f;
+    static constexpr bool kTrackError = true;
+    // The estimate in double: its absolute form (units of S^2) reaches
+    // 2^-105 |w|^2, below FP32's range.
+    using E = double;
+    static constexpr E kEps2 = 2.465190328815662e-32; // 2 * (2^-53)^2
+    static constexpr E kErrMax = 1e300;
+    static constexpr int kRatioClamp = 2000;
     using Z = double;
     MBX_HD static V2 make2(double a, double b) { return make_double2(a, b); }
     MBX_HD static float tof(double x) { return (float)x; }
+    MBX_HD static double toe(double x) { return x; }
     MBX_HD static double z(double x) { return x; }
     MBX_HD static double zabs2(double a, double b) { return a * a + b * b; }
 };
@@ -183,14 +197,19 @@ struct LaneReal<df32> {
     using V2 = df2;
     static constexpr float kTinyX = 1e-30f;         // as the FP32 lane: both parts must stay normal
     static constexpr float kMinS = 8.673617e-19f;   // 2^-60
+    static constexpr float kWFloor = 1e-30f;
     static constexpr float kEscLo = 0.999998f;     // screens run on the high parts, as in the FP32 lane
     static constexpr float kEscHi = 1.000002f;
     static constexpr int kExpClamp = 120;
     static constexpr bool kTrackError = true;
-    static constexpr float kEps2 = 2.524355e-29f;   // 2 * (2^-48)^2
+    using E = float;
+    static constexpr E kEps2 = 2.524355e-29f;   // 2 * (2^-48)^2
+    static constexpr E kErrMax = 3e38f;
+    static constexpr int kRatioClamp = 300;
     using Z = float;
     MBX_HD static V2 make2(df32 a, df32 b) { return df2{a, b}; }
     MBX_HD static float tof(df32 x) { return x.hi; }
+    MBX_HD static float toe(df32 x) { return x.hi; }
     MBX_HD static float z(df32 x) { return x.hi; }
     MBX_HD static float zabs2(df32 a, df32 b) { return a.hi * a.hi + b.hi * b.hi; }
 };
@@ -400,10 +419,11 @@ constexpr float kLaneCap2 = 0.25f;         // (1/2)^2
 
 // Squared relative error estimate of the delta.
 template <class T>
-MBX_HD float lane_rel_err2(float err2, T wr, T wi) {
-    const float a = LaneReal<T>::tof(wr), b = LaneReal<T>::tof(wi);
-    const float wm2 = a * a + b * b;
-    return wm2 > 0.0f ? err2 / wm2 : 0.0f;
+MBX_HD typename LaneReal<T>::E lane_rel_err2(typename LaneReal<T>::E err2, T wr, T wi) {
+    using E = typename LaneReal<T>::E;
+    const E a = LaneReal<T>::toe(wr), b = LaneReal<T>::toe(wi);
+    const E wm2 = a * a + b * b;
+    return wm2 > E(0) ? err2 / wm2 : E(0);
 }
 template <class V2>
 MBX_HD float lane_abs2f(V2 v) {
@@ -425,7 +445,7 @@ struct Lane {
     V2 Xc;               // X_m
     // running rounding-error estimate: err2 = (error of w)^2 in units of S^2,
     // g2 = |2 z|^2 at the current iterate (the step's error amplification)
-    float err2, g2;
+    typename LaneReal<T>::E err2, g2;
     // interior detection
     float zsr_f, zsi_f, conf_D2;
     T swr, swi;
@@ -523,13 +543,16 @@ MBX_HDF void lane_setup(Lane<T>& L, int i, const DeviceFrame& f, const MixedPara
     lane_setup_at(L, i, arr, p, dxf, dyf, orb);
 }
 
-// (a / b)^2 as float, saturating: converts err2 from units of a^2 to b^2.
+// (a / b)^2 in the estimate's type, saturating: converts err2 from units of
+// a^2 to b^2.
 template <class T>
-MBX_HD float lane_scale_ratio2(TE<T> a, TE<T> b) {
-    const float bm = LaneReal<T>::tof(b.m);
-    if (bm == 0.0f) return 0.0f;
-    const float r = LaneReal<T>::tof(a.m) / bm;
-    return ldexp_ftz(r * r, imax(-300, imin(300, 2 * (a.e - b.e))));
+MBX_HD typename LaneReal<T>::E lane_scale_ratio2(TE<T> a, TE<T> b) {
+    using E = typename LaneReal<T>::E;
+    constexpr int c = LaneReal<T>::kRatioClamp;
+    const E bm = LaneReal<T>::toe(b.m);
+    if (bm == E(0)) return E(0);
+    const E r = LaneReal<T>::toe(a.m) / bm;
+    return ldexp_ftz(r * r, imax(-c, imin(c, 2 * (a.e - b.e))));
 }
 
 // z = X_m + S w in FP64 (rare decisions).
@@ -541,12 +564,22 @@ MBX_HD void lane_z_double(const Lane<T>& L, const double2* Zd, double& zr, doubl
     zi = Xd.y + sd * (double)L.wi;
 }
 
+// The FP32 lane's step w' = (2 X + s w) w + d and its error update (one
+// rounding variance added, the existing error carried by g2 = |2 z|^2).
+MBX_HD void lane_step_f(float2 X, float s, float wr, float wi, float dr, float di, float err2, float g2, float& nwr, float& nwi, float& nerr2) {
+    const float fR = 2.0f * X.x + s * wr;
+    const float fI = 2.0f * X.y + s * wi;
+    nwr = fR * wr - fI * wi + dr;
+    nwi = fR * wi + fI * wr + di;
+    nerr2 = err2 * g2 + LaneReal<float>::kEps2 * (nwr * nwr + nwi * nwi);
+}
+
 // Interior decision: a lane whose error estimate is too large leaves for the
 // next tier (4: an interior decision it cannot vouch for) instead of reporting
 // interior (2).
 template <class T>
 MBX_HD int lane_interior(const Lane<T>& L) {
-    if (LaneReal<T>::kTrackError && lane_rel_err2(L.err2, L.wr, L.wi) > kLaneInteriorTol2) return 4;
+    if (LaneReal<T>::kTrackError && !(lane_rel_err2(L.err2, L.wr, L.wi) <= kLaneInteriorTol2)) return 4;
     return 2;
 }
 
@@ -570,6 +603,46 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     const Z ESC2z = (Z)g.ESC2;
     const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
     for (int b = 0; b < budget; ++b) {
+        if constexpr (std::is_same<T, float>::value) {
+            // Common steps of an FP32 lane without interior detection: an
+            // iteration that takes none of the branches below (no BLA position,
+            // orbit entry in range, no escape screen, precision cap, rescale,
+            // rebase candidate or end of the reference) is the step, the error
+            // update and the index advance. Such iterations run here with the
+            // same operations; the first iteration that could take a branch is
+            // left uncommitted and the general code redoes it from the same state.
+            if (!(INTR && p.use_interior)) {
+                const float wmax2 = p.wmax2, wmin2 = p.wmin2;
+                for (;;) {
+                    if (L.iter >= g.mxit) break;
+                    if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) break;
+                    if (fabsf(L.Xc.x) < R::kTinyX && fabsf(L.Xc.y) < R::kTinyX) break; // also m = 0 (X = 0)
+                    int nrm = L.rm + 1;
+                    if (per && nrm == per) nrm = 0;
+                    const float2 X = orb[nrm];
+                    float nwr, nwi, nerr2;
+                    lane_step_f(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
+                    const float zr = X.x + L.s * nwr, zi = X.y + L.s * nwi;
+                    const float zrad = zr * zr + zi * zi;
+                    const float wm2 = nwr * nwr + nwi * nwi;
+                    const float xr2 = X.x * X.x + X.y * X.y;
+                    const bool far = xr2 > R::kTinyX * R::kTinyX && L.s * L.s * wm2 < 0.2f * xr2;
+                    const bool rare = zrad > ESC2lo || (wm2 > 0.0f && !(nerr2 <= kLaneCap2 * wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > 0.0f) || !far ||
+                                      (!per && L.m + 1 >= reflen);
+                    if (rare) break;
+                    L.wr = nwr;
+                    L.wi = nwi;
+                    L.err2 = nerr2;
+                    L.g2 = 4.0f * zrad;
+                    ++L.m;
+                    ++L.iter;
+                    L.rm = nrm;
+                    L.Xc = X;
+                    ++n_steps;
+                    if (++b >= budget) return 0;
+                }
+            }
+        }
         if (L.iter >= g.mxit) return lane_interior(L);
         if (INTR && p.use_interior) {
             const int idxs = per ? L.rm : L.m;
@@ -618,15 +691,23 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         const bool tiny = (L.m == 0 && !(L.s >= R::kMinS)) ||
                           (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0));
         if (!tiny) {
-            const T fR = T(2) * L.Xc.x + L.s * L.wr;
-            const T fI = T(2) * L.Xc.y + L.s * L.wi;
-            const T nwr = fR * L.wr - fI * L.wi + L.dr;
-            const T nwi = fR * L.wi + fI * L.wr + L.di;
-            L.wr = nwr;
-            L.wi = nwi;
-            if (R::kTrackError) {
-                const float a = R::tof(nwr), c = R::tof(nwi);
-                L.err2 = L.err2 * L.g2 + R::kEps2 * (a * a + c * c);
+            if constexpr (std::is_same<T, float>::value) {
+                float nwr, nwi, nerr2;
+                lane_step_f(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
+                L.wr = nwr;
+                L.wi = nwi;
+                L.err2 = nerr2;
+            } else {
+                const T fR = T(2) * L.Xc.x + L.s * L.wr;
+                const T fI = T(2) * L.Xc.y + L.s * L.wi;
+                const T nwr = fR * L.wr - fI * L.wi + L.dr;
+                const T nwi = fR * L.wi + fI * L.wr + L.di;
+                L.wr = nwr;
+                L.wi = nwi;
+                if (R::kTrackError) {
+                    const typename R::E a = R::toe(nwr), c = R::toe(nwi);
+                    L.err2 = L.err2 * L.g2 + R::kEps2 * (a * a + c * c);
+                }
             }
         } else if constexpr (std::is_same<T, float>::value) {
             ++n_exact;
@@ -664,7 +745,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 const FE z2 = fe_add(fe_mul(zr, zr), fe_mul(zi, zi));
                 const FE q = fe_div(S0, S);
                 const double amp = S.m == 0.0 ? 0.0 : 4.0 * fe_to_double(fe_mul(z2, fe_mul(q, q)));
-                L.err2 = (float)fmin(amp * (double)L.err2, 3e38) + R::kEps2;
+                L.err2 = (typename R::E)fmin(amp * (double)L.err2, (double)R::kErrMax) + R::kEps2;
             }
             L.S = te_from_fe<T>(S);
             L.wr = (T)wr;
@@ -695,8 +776,8 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     // doubled) cannot carry |z_N|^2 or |z_(N-1)|^2 across the bailout.
                     const float sf = R::tof(L.s), wrf = R::tof(L.wr), wif = R::tof(L.wi), zf = (float)zesc, Ef = (float)ESC2z;
                     const float dzm2 = sf * sf * (wrf * wrf + wif * wif);
-                    const float amb = 4.0f * sqrtf(lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
-                    if (zf < Ef * (1.0f + amb) || 0.25f * L.g2 > Ef * (1.0f - amb)) return 3;
+                    const float amb = 4.0f * sqrtf((float)lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
+                    if (!(zf >= Ef * (1.0f + amb)) || !(0.25f * L.g2 <= Ef * (1.0f - amb))) return 3; // (a NaN estimate fails too)
                 }
                 return 1;
             }
@@ -750,18 +831,22 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 }
             }
         }
-        if (R::kTrackError) L.g2 = 4.0f * (float)zrad;
+        if (R::kTrackError) L.g2 = 4.0f * (typename R::E)zrad;
         // keep |w| ~ 1 (rescale window [1/wmax2, wmax2], autotuned); the scale
         // factor only needs to be near |w|, as long as S and w change by it
         // and its exact reciprocal
         const Z wm2 = R::zabs2(L.wr, L.wi);
-        if (R::kTrackError && wm2 > Z(0) && L.err2 > kLaneCap2 * (float)wm2) return 3; // precision spent
+        if (R::kTrackError && wm2 > Z(0) && !(L.err2 <= kLaneCap2 * (typename R::E)wm2)) return 3; // precision spent (or a NaN estimate)
         if (wm2 > Z(p.wmax2) || (wm2 < Z(p.wmin2) && wm2 > Z(0))) {
+            // |w| fell below the type's floor in one step (a near-zero |2 z|):
+            // the absolute estimate err2 ~ |w|^2 may have left the normal range
+            if (R::kTrackError && wm2 < Z(R::kWFloor)) return 3;
             const T wmag = T(tsqrt(wm2)), inv = T(1) / wmag;
             L.S = te_mulr(L.S, wmag);
             L.wr *= inv;
             L.wi *= inv;
-            if (R::kTrackError) L.err2 *= R::tof(inv) * R::tof(inv);
+            // err2 in the new units: err2 inv^2 = err2 / |w|^2 (no overflow of inv^2)
+            if (R::kTrackError) L.err2 = L.err2 / (typename R::E)wm2;
             lane_refresh(L);
         }
         // Rebase (mp.cpp:3584-3615): |z|^2 < |dz|^2 decided on floatexp with a

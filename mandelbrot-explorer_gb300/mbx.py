@@ -112,6 +112,7 @@ class Stats(ctypes.Structure):
         ("rerun_fp64_gpu_ms", ctypes.c_double),
         ("exact_steps", ctypes.c_longlong),
         ("fe_rebases", ctypes.c_longlong),
+        ("exact_reruns", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -357,7 +358,7 @@ class CudaComputeBackend:
             raise RuntimeError("autotune failed (%d): %s" % (rc, self.last_error()))
         return t.as_dict()
 
-    def set_tuning(self, threads=256, blocks_per_sm=3, smem_orbit_limit=200 * 1024, rescale_window=1e16):
+    def set_tuning(self, threads=256, blocks_per_sm=3, smem_orbit_limit=0, rescale_window=1e16):
         rc = self._lib.mbx_set_tuning(self._ctx, threads, blocks_per_sm, smem_orbit_limit, rescale_window)
         if rc != OK:
             raise RuntimeError("set_tuning failed (%d)" % rc)

@@ -40,16 +40,18 @@ def test_unknown_backend_name_rejected():
         mbx.create_compute_backend("d3d11")
 
 
-def test_request_layout_matches_header(tmp_path):
-    """The binding's mbx_request mirror has the header's size and field offsets."""
+@pytest.mark.parametrize("cname,pytype", [("mbx_request", "_Request"), ("mbx_stats", "Stats")])
+def test_struct_layout_matches_header(tmp_path, cname, pytype):
+    """The binding's struct mirrors have the header's sizes and field offsets."""
+    cls = getattr(mbx, pytype)
     src = tmp_path / "layout.c"
-    fields = [f for f, _ in mbx._Request._fields_]
-    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "mbx_gb300.h"\nint main(void){printf("%zu", sizeof(mbx_request));'
-                   + "".join('printf(" %%zu", offsetof(mbx_request, %s));' % f for f in fields) + "return 0;}\n")
+    fields = [f for f, _ in cls._fields_]
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "mbx_gb300.h"\nint main(void){printf("%%zu", sizeof(%s));' % cname
+                   + "".join('printf(" %%zu", offsetof(%s, %s));' % (cname, f) for f in fields) + "return 0;}\n")
     exe = tmp_path / "layout"
     import subprocess
 
     subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     vals = [int(x) for x in subprocess.check_output([str(exe)], text=True).split()]
-    assert vals[0] == ctypes.sizeof(mbx._Request)
-    assert vals[1:] == [getattr(mbx._Request, f).offset for f in fields]
+    assert vals[0] == ctypes.sizeof(cls)
+    assert vals[1:] == [getattr(cls, f).offset for f in fields]

@@ -118,3 +118,37 @@ def test_mixed_on_parity_cases(backend):
             print("\n" + msg)
             assert cls <= max(1, mi.size // 1000), name
             assert same >= 0.999, name
+
+
+@pytest.mark.parametrize("window", [1e8, 1e12, 1e16])
+@pytest.mark.parametrize("bps", [3, 4])
+def test_every_autotuner_shape_keeps_accuracy(window, bps):
+    """The autotuner picks launch shapes and rescale windows by speed alone, so
+    each shape it may pick must hold the accuracy bar: the minibrot frames with
+    arbitrary-precision goldens (most samples need the rerun tiers) class-exact
+    and within the verify harness's |dmu| bound."""
+    from conftest import GOLDEN
+
+    cases = load_cases()
+    be = mbx.create_compute_backend("cuda")
+    try:
+        be.set_tuning(256, bps, 0, window)
+        for name in ("minibrot875", "extref875", "gui875"):
+            c = cases[name]
+            out = {}
+            for mode in (mbx.PRECISION_MIXED, mbx.PRECISION_EXACT):
+                req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"],
+                                         sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"], precision_mode=mode)
+                assert be.compute_status(req) == mbx.OK, be.last_error()
+                out[mode] = (req.iterations, req.escape_iteration)
+            mi, mn = out[mbx.PRECISION_MIXED]
+            ei, en = out[mbx.PRECISION_EXACT]
+            t = np.fromfile(os.path.join(GOLDEN, "truth_%s.f32" % name), dtype="<f4")
+            valid = (t > -5) & (mi > -5)
+            ext = valid & (t > -1.5) & (mi > -1.5)
+            assert int(np.sum((mi[valid] < -1.5) != (t[valid] < -1.5))) == 0, (name, window, bps)
+            assert float(np.max(np.abs(mi[ext].astype(np.float64) - t[ext]), initial=0.0)) <= TRUTH_TOL[name][0], (name, window, bps)
+            both = (mi > -5) & (ei > -5)
+            print("\n[shape %d bps, window %.0e] %s: N identical to the exact form %.4f" % (bps, window, name, np.mean(mn[both] == en[both])))
+    finally:
+        be.close()
