@@ -218,6 +218,8 @@ class Engine {
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
     DevBuf<Bla32> dbla32_;
+    DevBuf<BlaMaxR2> dblamax_;
+    bool blamax_ok_ = false; // dblamax_ holds the current reference's table
     DevBuf<BlaDF> dbladf_;
     DevBuf<df2> dZdf_;
     DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample lane cost

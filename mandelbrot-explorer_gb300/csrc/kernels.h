@@ -45,6 +45,14 @@ struct __align__(16) BlaEntry {
 using Bla32 = BlaEntry<float>;
 using BlaDF = BlaEntry<df32>;
 using Bla64 = BlaEntry<double>;
+// Per BLA position of the FP32 lane (orbit index s with s - 1 a multiple of
+// 2^minlevel): the largest radius^2 over the levels the lane tries there, as
+// mantissa + exponent of the FP32 table; m = 0 when no level has a radius. A
+// |dz|^2 at or above it fails every level's radius test.
+struct BlaMaxR2 {
+    float m;
+    int e;
+};
 
 // Reference orbit shadows in device memory (mp.h:295-371).
 struct OrbitView {
@@ -220,6 +228,7 @@ struct MixedParams {
     const double* dpy_tab = nullptr;
     const float* dpx_tabf = nullptr;
     const float* dpy_tabf = nullptr;
+    const BlaMaxR2* blamax = nullptr; // FP32 lane: index (s - 1) >> minlevel
     unsigned wide_from = 0;  // rerun passes launched in two widths: the 32-lane
                              // variant runs when the queue holds >= wide_from
                              // entries, the narrow one below (0: no selection)

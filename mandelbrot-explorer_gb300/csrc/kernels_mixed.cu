@@ -32,6 +32,26 @@ __global__ void k_bla_to_lane(const double* r2, const double4* ab, BlaEntry<T>* 
     if (i < n) out[i] = bla_entry<T>(r2[i], ab[i]);
 }
 
+// The FP32 lane's per-position radius maxima (BlaMaxR2): the levels lane_bla
+// tries at s, startp down to minlevel, as it orders them.
+__global__ void k_bla_maxr2(const BlaEntry<float>* t, BlaView b, BlaMaxR2* out, int nq) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int s = (q << b.minlevel) + 1;
+    const int maxp = b.nlev - 1;
+    int startp = (s == 1) ? maxp : ffs32(s - 1) - 1;
+    if (startp > maxp) startp = maxp;
+    BlaMaxR2 best{0.0f, 0};
+    for (int p = startp; p >= b.minlevel; --p) {
+        const int i = (s - 1) >> p;
+        if (i >= b.size[p]) continue;
+        const BlaEntry<float> e = t[b.off[p] + i];
+        if (e.r2m == 0.0f) continue;
+        if (best.m == 0.0f || e.r2e > best.e || (e.r2e == best.e && e.r2m > best.m)) best = BlaMaxR2{e.r2m, e.r2e};
+    }
+    out[q] = best;
+}
+
 __device__ __forceinline__ float tlog2(float x) { return log2f(x); }
 __device__ __forceinline__ double tlog2(double x) { return log2(x); }
 __device__ __forceinline__ float tlog2(df32 x) { return log2f(x.hi + x.lo); }
@@ -405,7 +425,13 @@ int Engine::prepare_mixed() {
         if (!ensure(dbla32_, (size_t)n) || !ensure(dbladf_, (size_t)n)) return MBX_E_NOMEM;
         k_bla_to_lane<float><<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbla32_.p, n);
         k_bla_to_lane<df32><<<(n + 255) / 256, 256, 0, st_>>>(dr2_.p, dab_.p, dbladf_.p, n);
-        stats_.kernel_launches += 2;
+        const int nq = (len >> bla_.minlevel) + 2;
+        if (!ensure(dblamax_, (size_t)nq)) return MBX_E_NOMEM;
+        k_bla_maxr2<<<(nq + 255) / 256, 256, 0, st_>>>(dbla32_.p, bla_, dblamax_.p, nq);
+        stats_.kernel_launches += 3;
+        blamax_ok_ = true;
+    } else {
+        blamax_ok_ = false;
     }
     return cuda_ok("mixed preparation");
 }
@@ -428,6 +454,7 @@ MixedParams Engine::mixed_params() const {
     p.smem_entries = orbit_len_;
     p.wmax2 = mixed_wmax2_;
     p.wmin2 = 1.0f / mixed_wmax2_;
+    p.blamax = blamax_ok_ ? dblamax_.p : nullptr;
     if (ddpxy_.p && dpxy_w_ == W_ * SUB_) {
         p.dpx_tab = ddpxy_.p;
         p.dpy_tab = ddpxy_.p + dpxy_w_;

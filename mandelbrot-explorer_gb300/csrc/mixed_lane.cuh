@@ -605,17 +605,31 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     for (int b = 0; b < budget; ++b) {
         if constexpr (std::is_same<T, float>::value) {
             // Common steps of an FP32 lane without interior detection: an
-            // iteration that takes none of the branches below (no BLA position,
+            // iteration that takes none of the branches below (no BLA skip,
             // orbit entry in range, no escape screen, precision cap, rescale,
             // rebase candidate or end of the reference) is the step, the error
             // update and the index advance. Such iterations run here with the
             // same operations; the first iteration that could take a branch is
             // left uncommitted and the general code redoes it from the same state.
+            // At a BLA position the per-position radius maximum decides: if
+            // |dz|^2 is not below it, every level fails and lane_bla would
+            // return 0, so the iteration is a common one.
             if (!(INTR && p.use_interior)) {
                 const float wmax2 = p.wmax2, wmin2 = p.wmin2;
+                const BlaMaxR2* bmax = p.blamax;
+                const int minlevel = f.bla.minlevel;
                 for (;;) {
                     if (L.iter >= g.mxit) break;
-                    if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) break;
+                    if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
+                        if (!bmax) break;
+                        const BlaMaxR2 r = bmax[(L.rm - 1) >> minlevel];
+                        if (r.m != 0.0f) {
+                            const float wc2 = L.wr * L.wr + L.wi * L.wi;
+                            if (wc2 == 0.0f) break;
+                            const F32E dz2 = te_norm(L.S.m * L.S.m * wc2, 2 * L.S.e); // as lane_bla forms it
+                            if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) break;
+                        }
+                    }
                     if (fabsf(L.Xc.x) < R::kTinyX && fabsf(L.Xc.y) < R::kTinyX) break; // also m = 0 (X = 0)
                     int nrm = L.rm + 1;
                     if (per && nrm == per) nrm = 0;
