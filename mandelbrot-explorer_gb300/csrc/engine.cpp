@@ -1585,9 +1585,18 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     cudaError_t e;
     cudaEventRecord(ev0_, st_);
     if (use_floatexp_) {
-        const FeParams p = fe_params(mx_ref_it);
+        FeParams p = fe_params(mx_ref_it);
         int blocks = std::min((n + threads - 1) / threads, nsm_ * 8);
-        e = launch_fe_pass(f, p, blocks, threads, st_);
+        if (exact_rerun_ && n <= nsm_ * 4) {
+            // the mixed form's leftovers: few samples with long dependency
+            // chains, each alone in a warp of its own block (one per SM while
+            // they fit), so neither divergence nor a shared FP64 pipe
+            // serialises them
+            p.one_lane_per_warp = 1;
+            e = launch_fe_pass(f, p, n, 32, st_);
+        } else {
+            e = launch_fe_pass(f, p, blocks, threads, st_);
+        }
     } else {
         Fp64Params p;
         p.g = geom();
