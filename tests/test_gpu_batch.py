@@ -70,3 +70,28 @@ def test_batch_device_outputs_and_invalid():
     assert be.compute_batch([_req(*frames[1]), bad]) == mbx.E_INVALID
     assert "request 1" in be.last_error()
     be.close()
+
+
+def test_batch_exact_form_leftovers_match_single_frames():
+    """The 1080p 1e-300 frame leaves a few samples that neither the FP32 nor the
+    double-float estimate vouches for; the batch hands them to the frame's exact
+    form after its graph, as mbx_compute does after its tiers: same samples,
+    same values."""
+    be = mbx.create_compute_backend("cuda")
+    frames = [(views.deep_view(300), 1920, 1080), (views.deep_view(1000), 160, 90)]
+    singles = []
+    for v, w, h in frames:
+        r = _req(v, w, h)
+        assert be.compute_status(r) == mbx.OK, be.last_error()
+        st = be.last_stats.as_dict()
+        assert st["exact_reruns"] == st["fp64_reruns_fp64"]
+        singles.append((r.iterations.copy(), r.escape_iteration.copy(), st["exact_reruns"]))
+    assert singles[0][2] > 0
+    reqs = [_req(v, w, h) for v, w, h in frames]
+    assert be.compute_batch(reqs) == mbx.OK, be.last_error()
+    bs = be.last_batch_stats.as_dict()
+    assert bs["exact_reruns"] == sum(s[2] for s in singles)
+    for (it, en, _), r in zip(singles, reqs):
+        assert np.array_equal(r.escape_iteration, en) and np.array_equal(r.iterations, it)
+    print("\n[batch] exact-form leftovers: %d" % bs["exact_reruns"])
+    be.close()
