@@ -125,6 +125,7 @@ struct Counters {
     unsigned int finished;               // mixed pass: entries finished or queued
     unsigned int gmp_flags;              // floatexp pass: entries flagged for the arbitrary-precision recompute
     unsigned int interior_flagged;       // lane passes: interior decisions queued for the next tier
+    unsigned int probe_hit;              // interior gate probe: set by the first interior decision (the probe then stops)
     unsigned long long exact_steps;      // lane passes: steps taken in floatexp (orbit or delta below the lane's range)
     unsigned long long fe_rebases;       // lane passes: rebases decided in floatexp
 };
@@ -230,6 +231,7 @@ struct MixedParams {
     const float* dpx_tabf = nullptr;
     const float* dpy_tabf = nullptr;
     const BlaMaxR2* blamax = nullptr; // FP32 lane: index (s - 1) >> minlevel
+    int probe_stop = 0;               // interior gate probe: stop at the first interior decision
     unsigned wide_from = 0;  // rerun passes launched in two widths: the 32-lane
                              // variant runs when the queue holds >= wide_from
                              // entries, the narrow one below (0: no selection)

@@ -154,9 +154,21 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
             }
         }
         if (__ballot_sync(0xffffffffu, live) == 0) break;
+        if (p.probe_stop && (rounds & 7u) == 0) {
+            // the gate's answer is settled once one sample is interior: the
+            // probe's samples are rendered again by the main pass
+            unsigned hit = 0;
+            if (lane_id == 0) hit = *(volatile unsigned*)&f.ctr->probe_hit;
+            if (__shfl_sync(0xffffffffu, hit, 0)) {
+                exhausted = true;
+                live = false;
+                break;
+            }
+        }
         if (live) {
             T zrad = T(0);
             const int st = lane_run<T, INTR>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
+            if (p.probe_stop && (st == 2 || st == 4)) atomicExch(&f.ctr->probe_hit, 1u);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
                 // smooth value N - log2(log2|z|) in the lane type (the output is FP32)
@@ -272,14 +284,24 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
                         entry_coords(a.views[v].f.px, (int)(g - s_base[v]), arr);
                     }
                     const ViewDesc& vd = a.views[v];
-                    lane_setup_at(L, (int)g, arr, vd.p, te_from_fe<T>(vd.p.dxfe), te_from_fe<T>(vd.p.dyfe), ViewTables<T>::orb(vd));
-                    cost0 = (unsigned)(n_steps + 4 * n_bla);
-                    view = v;
-                    live = true;
+                    if (a.view_interior && !vd.f.out.cost && *(volatile const unsigned*)&a.view_interior[v] != 0u) {
+                        // the probe of a view whose gate is settled (an interior
+                        // sample found): its samples are rendered again by the main pass
+                        ++n_fin;
+                    } else {
+                        lane_setup_at(L, (int)g, arr, vd.p, te_from_fe<T>(vd.p.dxfe), te_from_fe<T>(vd.p.dyfe), ViewTables<T>::orb(vd));
+                        cost0 = (unsigned)(n_steps + 4 * n_bla);
+                        view = v;
+                        live = true;
+                    }
                 }
             }
         }
         if (__ballot_sync(0xffffffffu, live) == 0) break;
+        if (live && a.view_interior && (rounds & 7u) == 0 && !a.views[view].f.out.cost && *(volatile const unsigned*)&a.view_interior[view] != 0u) {
+            ++n_fin; // this view's gate is settled
+            live = false;
+        }
         if (live) {
             const ViewDesc& vd = a.views[view];
             const BlaEntry<T>* bt = vd.f.bla.use ? ViewTables<T>::bla(vd) : nullptr;
@@ -473,6 +495,9 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
     const size_t smem = p.orbit_in_smem ? bytes : 0;
     DeviceFrame g = f;
     if (!(bla_.use && dbla32_.p)) g.bla.use = 0;
+    // the interior gate's probe stops at its first interior decision (unless
+    // its per-sample costs are wanted)
+    p.probe_stop = (probe_gate_only_ && !g.out.cost) ? 1 : 0;
     auto launch = [&](auto kern) -> cudaError_t {
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
