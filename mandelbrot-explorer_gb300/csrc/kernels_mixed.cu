@@ -517,7 +517,7 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
 }
 
 // The double-float lane pass over the mixed pass's queue (entry count read on
-// the device). Its own queue feeds the FP64 lane pass.
+// the device). What it cannot vouch for, it queues for the exact form.
 cudaError_t Engine::run_df_pass(const DeviceFrame& f) {
     MixedParams p = mixed_params();
     const size_t bytes = ((size_t)orbit_len_ * 16 + 15) & ~(size_t)15;
