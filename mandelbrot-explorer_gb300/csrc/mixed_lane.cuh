@@ -564,14 +564,18 @@ MBX_HD void lane_z_double(const Lane<T>& L, const double2* Zd, double& zr, doubl
     zi = Xd.y + sd * (double)L.wi;
 }
 
-// The FP32 lane's step w' = (2 X + s w) w + d and its error update (one
-// rounding variance added, the existing error carried by g2 = |2 z|^2).
-MBX_HD void lane_step_f(float2 X, float s, float wr, float wi, float dr, float di, float err2, float g2, float& nwr, float& nwi, float& nerr2) {
-    const float fR = 2.0f * X.x + s * wr;
-    const float fI = 2.0f * X.y + s * wi;
+// The lane's step w' = (2 X + s w) w + d and its error update (one rounding
+// variance added, the existing error carried by g2 = |2 z|^2).
+template <class T>
+MBX_HD void lane_step(typename LaneReal<T>::V2 X, T s, T wr, T wi, T dr, T di, typename LaneReal<T>::E err2, typename LaneReal<T>::E g2, T& nwr, T& nwi,
+                      typename LaneReal<T>::E& nerr2) {
+    using R = LaneReal<T>;
+    const T fR = T(2) * X.x + s * wr;
+    const T fI = T(2) * X.y + s * wi;
     nwr = fR * wr - fI * wi + dr;
     nwi = fR * wi + fI * wr + di;
-    nerr2 = err2 * g2 + LaneReal<float>::kEps2 * (nwr * nwr + nwi * nwi);
+    const typename R::E a = R::toe(nwr), c = R::toe(nwi);
+    nerr2 = err2 * g2 + R::kEps2 * (a * a + c * c);
 }
 
 // Interior decision: a lane whose error estimate is too large leaves for the
@@ -603,8 +607,8 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     const Z ESC2z = (Z)g.ESC2;
     const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
     for (int b = 0; b < budget; ++b) {
-        if constexpr (std::is_same<T, float>::value) {
-            // Common steps of an FP32 lane without interior detection: an
+        if constexpr (!std::is_same<T, double>::value) {
+            // Common steps of a lane without interior detection: an
             // iteration that takes none of the branches below (no BLA skip,
             // orbit entry in range, no escape screen, precision cap, rescale,
             // rebase candidate or end of the reference) is the step, the error
@@ -615,8 +619,9 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
             // |dz|^2 is not below it, every level fails and lane_bla would
             // return 0, so the iteration is a common one.
             if (!(INTR && p.use_interior)) {
-                const float wmax2 = p.wmax2, wmin2 = p.wmin2;
-                const BlaMaxR2* bmax = p.blamax;
+                using E = typename R::E;
+                const Z wmax2 = Z(p.wmax2), wmin2 = Z(p.wmin2);
+                const BlaMaxR2* bmax = std::is_same<T, float>::value ? p.blamax : nullptr; // FP32 tables only
                 const int minlevel = f.bla.minlevel;
                 for (;;) {
                     if (L.iter >= g.mxit) break;
@@ -624,30 +629,32 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                         if (!bmax) break;
                         const BlaMaxR2 r = bmax[(L.rm - 1) >> minlevel];
                         if (r.m != 0.0f) {
-                            const float wc2 = L.wr * L.wr + L.wi * L.wi;
-                            if (wc2 == 0.0f) break;
-                            const F32E dz2 = te_norm(L.S.m * L.S.m * wc2, 2 * L.S.e); // as lane_bla forms it
+                            const Z wc2 = R::zabs2(L.wr, L.wi);
+                            if (wc2 == Z(0)) break;
+                            const TE<Z> dz2 = te_norm(R::z(L.S.m) * R::z(L.S.m) * wc2, 2 * L.S.e); // as lane_bla forms it
                             if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) break;
                         }
                     }
-                    if (fabsf(L.Xc.x) < R::kTinyX && fabsf(L.Xc.y) < R::kTinyX) break; // also m = 0 (X = 0)
+                    if (tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX) break; // also m = 0 (X = 0)
                     int nrm = L.rm + 1;
                     if (per && nrm == per) nrm = 0;
-                    const float2 X = orb[nrm];
-                    float nwr, nwi, nerr2;
-                    lane_step_f(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
-                    const float zr = X.x + L.s * nwr, zi = X.y + L.s * nwi;
-                    const float zrad = zr * zr + zi * zi;
-                    const float wm2 = nwr * nwr + nwi * nwi;
-                    const float xr2 = X.x * X.x + X.y * X.y;
-                    const bool far = xr2 > R::kTinyX * R::kTinyX && L.s * L.s * wm2 < 0.2f * xr2;
-                    const bool rare = zrad > ESC2lo || (wm2 > 0.0f && !(nerr2 <= kLaneCap2 * wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > 0.0f) || !far ||
+                    const typename R::V2 X = orb[nrm];
+                    T nwr, nwi;
+                    E nerr2;
+                    lane_step<T>(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
+                    const T zr = X.x + L.s * nwr, zi = X.y + L.s * nwi;
+                    const Z zrad = R::zabs2(zr, zi);
+                    const Z wm2 = R::zabs2(nwr, nwi);
+                    const Z xr2 = R::zabs2(X.x, X.y);
+                    const Z sz = R::z(L.s);
+                    const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * wm2 < Z(0.2) * xr2;
+                    const bool rare = zrad > ESC2lo || (wm2 > Z(0) && !(nerr2 <= kLaneCap2 * (E)wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > Z(0)) || !far ||
                                       (!per && L.m + 1 >= reflen);
                     if (rare) break;
                     L.wr = nwr;
                     L.wi = nwi;
                     L.err2 = nerr2;
-                    L.g2 = 4.0f * zrad;
+                    L.g2 = 4.0f * (E)zrad;
                     ++L.m;
                     ++L.iter;
                     L.rm = nrm;
@@ -705,24 +712,12 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         const bool tiny = (L.m == 0 && !(L.s >= R::kMinS)) ||
                           (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0));
         if (!tiny) {
-            if constexpr (std::is_same<T, float>::value) {
-                float nwr, nwi, nerr2;
-                lane_step_f(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
-                L.wr = nwr;
-                L.wi = nwi;
-                L.err2 = nerr2;
-            } else {
-                const T fR = T(2) * L.Xc.x + L.s * L.wr;
-                const T fI = T(2) * L.Xc.y + L.s * L.wi;
-                const T nwr = fR * L.wr - fI * L.wi + L.dr;
-                const T nwi = fR * L.wi + fI * L.wr + L.di;
-                L.wr = nwr;
-                L.wi = nwi;
-                if (R::kTrackError) {
-                    const typename R::E a = R::toe(nwr), c = R::toe(nwi);
-                    L.err2 = L.err2 * L.g2 + R::kEps2 * (a * a + c * c);
-                }
-            }
+            T nwr, nwi;
+            typename R::E nerr2;
+            lane_step<T>(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
+            L.wr = nwr;
+            L.wi = nwi;
+            L.err2 = nerr2;
         } else if constexpr (std::is_same<T, float>::value) {
             ++n_exact;
             const F32E S0 = L.S;
