@@ -93,7 +93,7 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
 // LANES < 32: only the low LANES lanes of a warp take samples. The rerun
 // passes are latency-bound (few samples, long dependency chains), so spreading
 // their samples over more warps hides more latency than filling each warp.
-template <class T, int MAXT, int MINB, int LANES = 32, bool INTR = true>
+template <class T, int MAXT, int MINB, int LANES = 32, bool INTR = true, bool FASTI = false>
 __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedParams p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orbit) {
     using V2 = typename LaneReal<T>::V2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         }
         if (live) {
             T zrad = T(0);
-            const int st = lane_run<T, INTR>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
+            const int st = lane_run<T, INTR, FASTI>(L, 32, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (p.probe_stop && (st == 2 || st == 4)) atomicExch(&f.ctr->probe_hit, 1u);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
@@ -506,6 +506,8 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
         kern<<<blocks, threads, smem, st_>>>(g, p, dbla32_.p, dZf_.p);
         return cudaGetLastError();
     };
+    if (probe_gate_only_ && threads == 256 && mixed_blocks_per_sm_ == 3) // the probe: common iterations in the fast loop too
+        return launch(k_lane_pass<float, 256, 3, 32, true, true>);
     if (!p.use_interior) { // exterior after the probe: the lane without interior detectors
         if (mixed_blocks_per_sm_ >= 4) return launch(k_lane_pass<float, 256, 4, 32, false>);
         if (mixed_blocks_per_sm_ == 3) return launch(k_lane_pass<float, 256, 3, 32, false>);

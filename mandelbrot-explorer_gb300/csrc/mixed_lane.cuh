@@ -593,7 +593,7 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 // INTR = false compiles the lane without its interior detectors, for passes
 // whose interior detection is off (exterior frames after the probe): their
 // state then takes no registers.
-template <class T, bool INTR = true>
+template <class T, bool INTR = true, bool FASTI = false>
 MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
                      int reflen, T ESC2f, int blamask, T& zrad_out, unsigned& n_steps, unsigned& n_bla, unsigned long long& n_skip,
                      unsigned& n_rebase, unsigned& n_exact, unsigned& n_ferebase) {
@@ -618,13 +618,23 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
             // At a BLA position the per-position radius maximum decides: if
             // |dz|^2 is not below it, every level fails and lane_bla would
             // return 0, so the iteration is a common one.
-            if (!(INTR && p.use_interior)) {
+            // FASTI: the common-iteration loop with interior detection on
+            // too (the interior gate's probe); its extra tests: no state
+            // repetition, no save due, no confirmation in progress and not a
+            // 16th-iteration Brent check
+            const bool intr = INTR && p.use_interior;
+            if (!intr || FASTI) {
                 using E = typename R::E;
                 const Z wmax2 = Z(p.wmax2), wmin2 = Z(p.wmin2);
                 const BlaMaxR2* bmax = std::is_same<T, float>::value ? p.blamax : nullptr; // FP32 tables only
                 const int minlevel = f.bla.minlevel;
                 for (;;) {
                     if (L.iter >= g.mxit) break;
+                    if (FASTI && intr) {
+                        const int idxs = per ? L.rm : L.m;
+                        if (idxs == L.sidx && L.wr == L.swr && L.wi == L.swi && L.S.m == L.sS.m && L.S.e == L.sS.e) break;
+                        if (L.iter - L.save_iter2 >= L.twin2 || L.conf_P > 0 || (((L.iter + 1) & 15) == 0 && L.conf_giveup < 3)) break;
+                    }
                     if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
                         if (!bmax) break;
                         const BlaMaxR2 r = bmax[(L.rm - 1) >> minlevel];
