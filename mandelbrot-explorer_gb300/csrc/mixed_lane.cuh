@@ -628,14 +628,24 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 const Z wmax2 = Z(p.wmax2), wmin2 = Z(p.wmin2);
                 const BlaMaxR2* bmax = std::is_same<T, float>::value ? p.blamax : nullptr; // FP32 tables only
                 const int minlevel = f.bla.minlevel;
+                // one counter: m; iter = m + off, the steps taken and the
+                // budget spent follow from m - m0 and are written back on exit.
+                // m reaching mlim covers maxiter and the end of a non-periodic
+                // reference (m + 1 >= reflen, where the rebase is forced).
+                const int m0 = L.m, off = L.iter - L.m;
+                int mlim = g.mxit - off;
+                if (!per && reflen - 1 < mlim) mlim = reflen - 1;
+                const int mbud = m0 + (budget - b);
+                int m = m0;
                 for (;;) {
-                    if (L.iter >= g.mxit) break;
+                    if (m >= mlim) break;
                     if (FASTI && intr) {
-                        const int idxs = per ? L.rm : L.m;
+                        const int it = m + off;
+                        const int idxs = per ? L.rm : m;
                         if (idxs == L.sidx && L.wr == L.swr && L.wi == L.swi && L.S.m == L.sS.m && L.S.e == L.sS.e) break;
-                        if (L.iter - L.save_iter2 >= L.twin2 || L.conf_P > 0 || (((L.iter + 1) & 15) == 0 && L.conf_giveup < 3)) break;
+                        if (it - L.save_iter2 >= L.twin2 || L.conf_P > 0 || (((it + 1) & 15) == 0 && L.conf_giveup < 3)) break;
                     }
-                    if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
+                    if (blat && m >= 2 && ((L.rm - 1) & blamask) == 0) {
                         if (!bmax) break;
                         const BlaMaxR2 r = bmax[(L.rm - 1) >> minlevel];
                         if (r.m != 0.0f) {
@@ -658,20 +668,22 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     const Z xr2 = R::zabs2(X.x, X.y);
                     const Z sz = R::z(L.s);
                     const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * wm2 < Z(0.2) * xr2;
-                    const bool rare = zrad > ESC2lo || (wm2 > Z(0) && !(nerr2 <= kLaneCap2 * (E)wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > Z(0)) || !far ||
-                                      (!per && L.m + 1 >= reflen);
+                    const bool rare = zrad > ESC2lo || (wm2 > Z(0) && !(nerr2 <= kLaneCap2 * (E)wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > Z(0)) || !far;
                     if (rare) break;
                     L.wr = nwr;
                     L.wi = nwi;
                     L.err2 = nerr2;
                     L.g2 = 4.0f * (E)zrad;
-                    ++L.m;
-                    ++L.iter;
+                    ++m;
                     L.rm = nrm;
                     L.Xc = X;
-                    ++n_steps;
-                    if (++b >= budget) return 0;
+                    if (m >= mbud) break;
                 }
+                L.m = m;
+                L.iter = m + off;
+                n_steps += (unsigned)(m - m0);
+                b += m - m0;
+                if (b >= budget) return 0;
             }
         }
         if (L.iter >= g.mxit) return lane_interior(L);
