@@ -636,6 +636,11 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 int mlim = g.mxit - off;
                 if (!per && reflen - 1 < mlim) mlim = reflen - 1;
                 const int mbud = m0 + (budget - b);
+                // |dz|^2 < |X|^2 / 5 (the rebase screen) as 5.0001 s^2 |w|^2 <
+                // |X|^2: the margin makes it imply the general code's form
+                // whatever the roundings, so a committed iteration is one the
+                // general code would not rebase
+                const Z s2x5 = Z(5.0001) * (R::z(L.s) * R::z(L.s));
                 int m = m0;
                 for (;;) {
                     if (m >= mlim) break;
@@ -666,9 +671,10 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     const Z zrad = R::zabs2(zr, zi);
                     const Z wm2 = R::zabs2(nwr, nwi);
                     const Z xr2 = R::zabs2(X.x, X.y);
-                    const Z sz = R::z(L.s);
-                    const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * wm2 < Z(0.2) * xr2;
-                    const bool rare = zrad > ESC2lo || (wm2 > Z(0) && !(nerr2 <= kLaneCap2 * (E)wm2)) || wm2 > wmax2 || (wm2 < wmin2 && wm2 > Z(0)) || !far;
+                    const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && s2x5 * wm2 < xr2;
+                    // (|w| = 0 and the precision cap both leave through the
+                    // |w|^2 tests: the general code handles them)
+                    const bool rare = zrad > ESC2lo || !(nerr2 <= kLaneCap2 * (E)wm2) || wm2 > wmax2 || wm2 < wmin2 || !far;
                     if (rare) break;
                     L.wr = nwr;
                     L.wi = nwi;
