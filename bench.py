@@ -167,7 +167,7 @@ def main():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--cpu-sample", default="1920x1080", help="cpu_baseline sample size (same views); one render of each")
     ap.add_argument("--ref-sample", default="960x540", help="--impl reference per-step sample size (same views)")
-    ap.add_argument("--plain-sample", default="480x270", help="plain FP64 GPU sample size (same views); 'full' for 1920x1080")
+    ap.add_argument("--plain-sample", default="full", help="plain FP64 GPU sample size (same views), WxH or 'full' (the frames' own size)")
     ap.add_argument("--profile", default=None, help="comma-separated view labels (e.g. 1e-300): render (and colour) only those, default launch shape, no baselines (for ncu captures)")
     ap.add_argument("--profile-batch", action="store_true", help="with --profile: render the views as one batch with the learned ordering training")
     args = ap.parse_args()
@@ -242,7 +242,9 @@ def main():
     outs = [(torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")) for _ in vlist]
     reruns = {}
 
-    def step(reuse=True):
+    per_frame = {v["label"]: dict(eff=0, steps=0, bla=0, gpu_ms=0.0, fp32_ms=0.0, fp32_steps=0, fp32_bla=0) for v in vlist}
+
+    def step(reuse=True, record=False):
         eff = steps = bla = launches = 0
         gpu_ms = 0.0
         per_view = []
@@ -256,6 +258,15 @@ def main():
             launches += st["kernel_launches"]
             gpu_ms += st["pass_gpu_ms"]
             reruns[v["label"]] = {"double_float": st["fp64_reruns"], "exact_form": st["exact_reruns"]}
+            if record:
+                pf = per_frame[v["label"]]
+                pf["eff"] += st["effective_iterations"]
+                pf["steps"] += st["steps"]
+                pf["bla"] += st["bla_applies"]
+                pf["gpu_ms"] += st["pass_gpu_ms"]
+                pf["fp32_ms"] += st["fp32_pass_gpu_ms"]
+                pf["fp32_steps"] += st["fp32_pass_steps"]
+                pf["fp32_bla"] += st["fp32_pass_bla_applies"]
         return eff, steps, bla, launches, gpu_ms, per_view
 
     # warm-up (the first step builds each frame's reference)
@@ -271,7 +282,7 @@ def main():
     tot = [0, 0, 0, 0, 0.0]
     frame_ms = np.zeros(len(vlist))
     for _ in range(args.steps):
-        eff, steps, bla, launches, gpu_ms, per_view = step(reuse=True)
+        eff, steps, bla, launches, gpu_ms, per_view = step(reuse=True, record=True)
         tot[0] += eff
         tot[1] += steps
         tot[2] += bla
@@ -364,15 +375,13 @@ def main():
                 "note": "mbx_colorize on device values (log-power palette, ss 1): 4 B read + 3 B written per pixel; compute-bound on the pair-of-floats log/pow"}
 
     # end to end: host buffers, fresh reference per frame, D2H inside
-    e2e_eff, e2e_t, h2d, d2h = 0, 0.0, 0, 0
+    e2e_eff, e2e_t = 0, 0.0
     host_frames = []
     for v in vlist:
         t = time.perf_counter()
         req, st = render(be, mbx, v, mbx.PRECISION_MIXED, reuse=False)
         e2e_t += time.perf_counter() - t
         e2e_eff += st["effective_iterations"]
-        h2d += st["reference_length"] * 16 * 3 + 64 * 1024  # orbit shadows (+ floatexp shadow) and tables, approx by construction
-        d2h += req.iterations.nbytes + req.escape_iteration.nbytes
         host_frames.append(req.escape_iteration.copy())
     e2e_value = e2e_eff / e2e_t / 1e9
     # the same step (both frames) as one mbx_compute_batch call with host
@@ -381,13 +390,18 @@ def main():
     bat2 = mbx.create_compute_backend("cuda", local)
     b_reqs = [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], W, H, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED) for v in vlist]
     assert bat2.compute_batch(b_reqs) == mbx.OK, bat2.last_error()  # allocations
-    eb_eff, eb_t = 0, 0.0
+    eb_eff, eb_t, h2d, d2h = 0, 0.0, 0, 0
     for _ in range(2):
         b_reqs = [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], W, H, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED) for v in vlist]
         t = time.perf_counter()
         assert bat2.compute_batch(b_reqs) == mbx.OK, bat2.last_error()
         eb_t += time.perf_counter() - t
         eb_eff += bat2.last_batch_stats.effective_iterations + sum(s_.effective_iterations for s_ in bat2.last_view_stats)
+        # bytes the library copied in this step, counted at each copy
+        h2d += bat2.last_batch_stats.h2d_bytes + sum(s_.h2d_bytes for s_ in bat2.last_view_stats)
+        d2h += bat2.last_batch_stats.d2h_bytes + sum(s_.d2h_bytes for s_ in bat2.last_view_stats)
+    h2d //= 2
+    d2h //= 2
     for q, hf in zip(b_reqs, host_frames):
         assert np.array_equal(q.escape_iteration, hf), "batched frames differ from single-frame renders"
     bat2.close()
@@ -412,9 +426,43 @@ def main():
         total += req_e.escape_iteration.size
     plain_value = plain_eff / plain_t / 1e9
 
-    # roofline of the dominant kernel (the mixed delta pass), FP32 pipe
+    # roofline: the dominant kernel (the FP32 lane passes, k_lane_pass<float>)
+    # on its own steps, BLA applies and CUDA-event time; beside it, every
+    # delta pass of the frames (all tiers) over the passes' time
     flops = FLOPS_PER_STEP * tot[1] + FLOPS_PER_BLA * tot[2]
-    achieved = flops / (tot[4] / 1e3) / 1e12 if tot[4] > 0 else 0.0
+    achieved_all = flops / (tot[4] / 1e3) / 1e12 if tot[4] > 0 else 0.0
+    k_ms = sum(pf["fp32_ms"] for pf in per_frame.values())
+    k_flops = sum(FLOPS_PER_STEP * pf["fp32_steps"] + FLOPS_PER_BLA * pf["fp32_bla"] for pf in per_frame.values())
+    achieved = k_flops / (k_ms / 1e3) / 1e12 if k_ms > 0 else 0.0
+    frames = {}
+    for v in vlist:
+        pf = per_frame[v["label"]]
+        sec = pf["gpu_ms"] / 1e3
+        frames[v["label"]] = {
+            "frame_ms": float(frame_ms[[u["label"] for u in vlist].index(v["label"])] / args.steps),
+            "pass_gpu_ms": pf["gpu_ms"] / args.steps,
+            "gpixel_iter_per_s": pf["eff"] / sec / 1e9 if sec > 0 else None,
+            "executed_steps_per_s": pf["steps"] / sec if sec > 0 else None,
+            "bla_applies_per_s": pf["bla"] / sec if sec > 0 else None,
+            "fp32_pass": {"gpu_ms": pf["fp32_ms"] / args.steps, "steps": pf["fp32_steps"] // args.steps, "bla_applies": pf["fp32_bla"] // args.steps,
+                          "tflops": (FLOPS_PER_STEP * pf["fp32_steps"] + FLOPS_PER_BLA * pf["fp32_bla"]) / (pf["fp32_ms"] / 1e3) / 1e12 if pf["fp32_ms"] > 0 else None},
+        }
+    # accuracy at the configuration: the timed frames' mixed-form outputs on
+    # each frame's committed arbitrary-precision truth subset (4096 samples,
+    # tests/golden/make_truth.py)
+    truth_acc = {}
+    for v, o in zip(vlist, outs):
+        tp = os.path.join(ROOT, "tests", "golden", "truth_c2_%s.npz" % v["label"])
+        if not os.path.exists(tp) or (W, H) != (1920, 1080):
+            continue
+        z = np.load(tp)
+        idx = torch.from_numpy(z["idx"].astype(np.int64)).cuda()
+        en = o[1][idx].cpu().numpy()
+        mu = o[0][idx].cpu().numpy().astype(np.float64)
+        tn, tv = z["N"], z["value"].astype(np.float64)
+        ext = (tn > 0) & (en > 0)
+        truth_acc[v["label"]] = {"samples": int(idx.numel()), "escape_iteration_identical": float(np.mean(en == tn)), "class_mismatch": int(np.sum((en < 0) != (tn < 0))),
+                                 "max_abs_dmu": float(np.max(np.abs(mu[ext] - tv[ext]), initial=0.0))}
 
     cpu = None
     if rank == 0:
@@ -442,6 +490,7 @@ def main():
                 "resolution": "%dx%d" % (W, H),
                 "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 16.6 MB written per frame; no flush",
                 "frame_ms": {v["label"]: float(ms / args.steps) for v, ms in zip(vlist, frame_ms)},
+                "frames": frames,
                 "autotuned": tuning,
                 "batched": batched,
                 "image_epilogue": epilogue,
@@ -453,8 +502,12 @@ def main():
             "plain_fp64": {"value": plain_value, "unit": UNIT, "sample": "%dx%d" % (pw, ph), "frame_ms_scaled_to_1080p": plain_frame_ms},
             "tuned_vs_plain": value / plain_value if plain_value > 0 else None,
             "learned_1e-1000_vs_plain": (plain_frame_ms[[v["label"] for v in vlist].index("1e-1000")] / batched["learned_order"]["frame_1e-1000_ms"]) if "frame_1e-1000_ms" in batched.get("learned_order", {}) else None,
-            "accuracy": {"escape_iteration_identical_vs_exact_fp64": agree / total if total else None, "class_mismatch": cls_mis, "samples": total},
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+            "accuracy": {"vs_truth": truth_acc,
+                         "vs_exact_fp64": {"escape_iteration_identical": agree / total if total else None, "class_mismatch": cls_mis, "samples": total}},
+            "roofline": {"bound": "fp32", "kernel": "k_lane_pass<float> (FP32 lane passes: probe + main)", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                         "algorithmic": "25 flops per executed delta step + 19 per BLA application (mp.cpp:2457-2469, 2558, 2732-2740), over the kernel's CUDA-event time",
+                         "all_passes": {"achieved": achieved_all, "frac": achieved_all / fp32_peak if fp32_peak else None, "note": "every delta pass of the frames (FP32, double-float and exact-form tiers) over their GPU time"},
                          "peak_source": "measured in-run FMA issue rate (mbx_measure_fma_peak); MEASURED_PEAKS.json holds only HBM and bf16", "fp64_peak": fp64_peak},
             "cpu_baseline": cpu,
             "clocks": clk,

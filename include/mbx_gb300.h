@@ -15,7 +15,7 @@
 extern "C" {
 #endif
 
-#define MBX_ABI_VERSION 2
+#define MBX_ABI_VERSION 3
 
 /* Coloring flags: same bit values as the reference's ColoringMethod enum
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
@@ -91,6 +91,10 @@ typedef struct {
     long long exact_steps;          /* mixed form: steps taken in floatexp (orbit or delta below the lane type's range) */
     long long fe_rebases;           /* mixed form: rebases decided in floatexp (inside the margin, end of reference) */
     long long exact_reruns;         /* mixed form: samples finished by the exact form (no tier could vouch for them; equals fp64_reruns_fp64) */
+    long long h2d_bytes, d2h_bytes; /* bytes copied host->device / device->host by the call (counted at each copy) */
+    double fp32_pass_gpu_ms;        /* mixed form: CUDA-event time of the FP32 lane passes alone (probe and main) */
+    long long fp32_pass_steps;      /* mixed form: delta steps executed by those passes */
+    long long fp32_pass_bla_applies;/* mixed form: BLA skips taken by those passes */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns
@@ -185,9 +189,12 @@ int mbx_schedule_gradient(mbx_context* ctx, const float* features, const float* 
  * the process exits; frames above 2,097,152 samples are rejected with
  * MBX_E_TOO_LARGE. The first call on each device resolves the array's device
  * address with that device current, so make that first call before any stream
- * capture. All calls share the one array: calls that overlap on the GPU race.
+ * capture. Every call waits for `stream` to finish before it returns. All
+ * calls share the one array: calls that overlap on the GPU race.
  * Coloring bits: MBX_EXTERIOR_DIST_EST and MBX_DE_OVERLAY only (no
- * supersampling). Calls no allocating CUDA or library routine. */
+ * supersampling); MBX_DE_OVERLAY needs the normal buffer, which receives the
+ * overlay distance (MBX_E_INVALID without it). Calls no allocating CUDA or
+ * library routine. */
 int mbx_render_shallow_noalloc(double c0_re, double c0_im, double dx, double dy, int width, int height, int max_iterations,
                                double bailout, int coloring_method, float* iterations, int32_t* escape_iteration,
                                float* normal, void* stream);

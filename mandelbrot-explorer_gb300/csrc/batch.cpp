@@ -331,6 +331,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
         cudaMemcpyAsync(d_main_total_, &h_main_total_, sizeof(unsigned), cudaMemcpyHostToDevice, st_);
         cudaMemcpyAsync(d_probe_, h_desc_, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
         cudaMemcpyAsync(d_main_, h_desc_ + nv, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
+        bs.h2d_bytes += (long long)(sizeof(unsigned) + 2 * sizeof(ViewDesc) * nv);
         rc = build_graph(nv, probe_total, main_total, cancel_flag, err);
         if (rc != MBX_OK) return rc;
         cudaEventRecord(ev0_, st_);
@@ -346,6 +347,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             return MBX_E_CANCELLED;
         }
         bs.pass_gpu_ms = ms;
+        bs.d2h_bytes += (long long)(4 * sizeof(Counters)); // the graph's counter readback
         bs.kernel_launches = 5; // probe FP32; gate; main FP32, double-float (two widths)
         bs.passes = 2;
         for (int c = 0; c < 4; ++c) {
@@ -383,6 +385,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             if (e != cudaSuccess) return cuda_fail(err, "double-float rerun readback", e);
             std::vector<unsigned> vint((size_t)nv);
             cudaMemcpyAsync(vint.data(), d_view_interior_, sizeof(unsigned) * nv, cudaMemcpyDeviceToHost, st_);
+            bs.d2h_bytes += (long long)(sizeof(uint64_t) * n_exact + sizeof(unsigned) * nv);
             e = cudaStreamSynchronize(st_);
             if (e != cudaSuccess) return cuda_fail(err, "interior gate readback", e);
             std::vector<std::vector<uint64_t>> per((size_t)nv);

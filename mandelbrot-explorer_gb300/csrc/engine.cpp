@@ -1242,15 +1242,15 @@ int Engine::upload_reference(int ref_it) {
     orbit_len_ = len;
     const double t0 = now_ms();
     if (!ensure(dZ_, (size_t)MXIT_ + 2) || !ensure(dzm3_, (size_t)MXIT_ + 2)) return MBX_E_NOMEM;
-    cudaMemcpyAsync(dZ_.p, hZ_.data(), sizeof(double2) * len, cudaMemcpyHostToDevice, st_);
-    cudaMemcpyAsync(dzm3_.p, hzm3_.data(), sizeof(double) * (MXIT_ + 1), cudaMemcpyHostToDevice, st_);
+    copy_async(dZ_.p, hZ_.data(), sizeof(double2) * len, cudaMemcpyHostToDevice);
+    copy_async(dzm3_.p, hzm3_.data(), sizeof(double) * (MXIT_ + 1), cudaMemcpyHostToDevice);
     if (use_floatexp_) {
         if (!ensure(dZfe_, (size_t)MXIT_ + 2)) return MBX_E_NOMEM;
-        cudaMemcpyAsync(dZfe_.p, hZfe_.data(), sizeof(FE2) * len, cudaMemcpyHostToDevice, st_);
+        copy_async(dZfe_.p, hZfe_.data(), sizeof(FE2) * len, cudaMemcpyHostToDevice);
     }
     if (deriv_) {
         if (!ensure(dD_, (size_t)MXIT_ + 2)) return MBX_E_NOMEM;
-        cudaMemcpyAsync(dD_.p, hD_.data(), sizeof(double2) * len, cudaMemcpyHostToDevice, st_);
+        copy_async(dD_.p, hD_.data(), sizeof(double2) * len, cudaMemcpyHostToDevice);
     }
     stats_.copy_ms += now_ms() - t0;
     return cuda_ok("orbit upload");
@@ -1284,7 +1284,7 @@ int Engine::build_bla(int reflen) {
     stats_.kernel_launches += bla_.nlev;
     if (e != cudaSuccess) return fail_cuda("bla build", e);
     unsigned long long bits = 0;
-    cudaMemcpyAsync(&bits, &dctr_->glitch_min_bits, sizeof(bits), cudaMemcpyDeviceToHost, st_);
+    copy_async(&bits, &dctr_->glitch_min_bits, sizeof(bits), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return fail_cuda("bla build", e);
     double rmax2;
@@ -1325,8 +1325,8 @@ int Engine::build_dc_tables() {
     dc_xoff_ = -xmin;
     dc_yoff_ = -ymin;
     if (!ensure(ddcx_, nx) || !ensure(ddcy_, ny)) return MBX_E_NOMEM;
-    cudaMemcpyAsync(ddcx_.p, hdcx_.data(), sizeof(double) * nx, cudaMemcpyHostToDevice, st_);
-    cudaMemcpyAsync(ddcy_.p, hdcy_.data(), sizeof(double) * ny, cudaMemcpyHostToDevice, st_);
+    copy_async(ddcx_.p, hdcx_.data(), sizeof(double) * nx, cudaMemcpyHostToDevice);
+    copy_async(ddcy_.p, hdcy_.data(), sizeof(double) * ny, cudaMemcpyHostToDevice);
     return cuda_ok("dc tables");
 }
 
@@ -1336,6 +1336,12 @@ int Engine::cuda_ok(const char* what) {
     if (e != cudaSuccess) return fail_cuda(what, e);
     return MBX_OK;
 }
+cudaError_t Engine::copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    if (kind == cudaMemcpyHostToDevice) stats_.h2d_bytes += (long long)bytes;
+    else if (kind == cudaMemcpyDeviceToHost) stats_.d2h_bytes += (long long)bytes;
+    return cudaMemcpyAsync(dst, src, bytes, kind, st_);
+}
+
 int Engine::fail_cuda(const char* what, cudaError_t e) {
     err_ = std::string(what) + ": " + cudaGetErrorString(e);
     return MBX_E_CUDA;
@@ -1409,7 +1415,7 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         n = (int)keys->size();
         if (n == 0) return MBX_OK;
         if (!ensure(dkeys_, n)) return MBX_E_NOMEM;
-        cudaMemcpyAsync(dkeys_.p, keys->data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st_);
+        copy_async(dkeys_.p, keys->data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice);
         px.keys = dkeys_.p;
         px.n = n;
         kept.swap(*keys);
@@ -1433,13 +1439,18 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         // the interior gate's probe: its samples are rendered again by the
         // main pass, so its queue is not rerun; its gate counts the interior
         // decisions the FP32 lane could not vouch for as interior
-        cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+        copy_async(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost);
         e = cudaStreamSynchronize(st_);
         stats_.kernel_ms += now_ms() - t0;
         if (e != cudaSuccess) return fail_cuda("mixed probe pass", e);
         float ms = 0.0f;
-        if (cudaEventElapsedTime(&ms, ev0_, evm_) == cudaSuccess) stats_.pass_gpu_ms += ms;
+        if (cudaEventElapsedTime(&ms, ev0_, evm_) == cudaSuccess) {
+            stats_.pass_gpu_ms += ms;
+            stats_.fp32_pass_gpu_ms += ms;
+        }
         if (cancel_.load()) return MBX_E_CANCELLED;
+        stats_.fp32_pass_steps += (long long)hctr_->steps;
+        stats_.fp32_pass_bla_applies += (long long)hctr_->bla_applies;
         hctr_->interior += hctr_->interior_flagged;
         stats_.steps += (long long)hctr_->steps;
         stats_.bla_applies += (long long)hctr_->bla_applies;
@@ -1466,16 +1477,23 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     stats_.kernel_launches += 2; // narrow and wide variants, one of which runs
     if (e != cudaSuccess) return fail_cuda("double-float rerun launch", e);
     cudaEventRecord(ev1_, st_);
-    cudaMemcpyAsync(hctr_, dctr_, 2 * sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    copy_async(hctr_, dctr_, 2 * sizeof(Counters), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("mixed pass", e);
     {
-        float ms = 0.0f, rms = 0.0f;
+        float ms = 0.0f, rms = 0.0f, fms = 0.0f;
         if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) stats_.pass_gpu_ms += ms;
         if (cudaEventElapsedTime(&rms, evm_, ev1_) == cudaSuccess) stats_.rerun_gpu_ms += rms;
+        if (cudaEventElapsedTime(&fms, ev0_, evm_) == cudaSuccess) stats_.fp32_pass_gpu_ms += fms;
+        stats_.fp32_pass_steps += (long long)hctr_[0].steps;
+        stats_.fp32_pass_bla_applies += (long long)hctr_[0].bla_applies;
     }
     if (cancel_.load()) return MBX_E_CANCELLED;
+    if ((hctr_[0].stage_timeouts | hctr_[1].stage_timeouts) >> 16) {
+        err_ = "orbit staging copy still in flight when its block finished";
+        return MBX_E_CUDA;
+    }
     Counters& a = hctr_[0];
     for (int k = 1; k < 2; ++k) {
         const Counters& b = hctr_[k];
@@ -1502,7 +1520,7 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         // A block left samples unstarted (orbit staging timed out): scan the
         // flags and take them through the FP64 floatexp pass.
         hdone_.resize(n);
-        cudaMemcpyAsync(hdone_.data(), ddone_.p, n, cudaMemcpyDeviceToHost, st_);
+        copy_async(hdone_.data(), ddone_.p, n, cudaMemcpyDeviceToHost);
         e = cudaStreamSynchronize(st_);
         if (e != cudaSuccess) return fail_cuda("pass readback", e);
         std::vector<uint64_t> pending;
@@ -1532,7 +1550,7 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         // recomputes) finishes them, so every sample carries either a vouched
         // result or the exact form's.
         std::vector<uint64_t> pending(n_exact);
-        cudaMemcpyAsync(pending.data(), drerun2_keys_.p, sizeof(uint64_t) * n_exact, cudaMemcpyDeviceToHost, st_);
+        copy_async(pending.data(), drerun2_keys_.p, sizeof(uint64_t) * n_exact, cudaMemcpyDeviceToHost);
         e = cudaStreamSynchronize(st_);
         if (e != cudaSuccess) return fail_cuda("double-float rerun readback", e);
         stats_.exact_reruns += (long long)n_exact;
@@ -1569,7 +1587,7 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
         px.n = n;
         if (n == 0) return MBX_OK;
         if (!ensure(dkeys_, n)) return MBX_E_NOMEM;
-        cudaMemcpyAsync(dkeys_.p, keys->data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st_);
+        copy_async(dkeys_.p, keys->data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice);
         px.keys = dkeys_.p;
     }
     if (n <= 0) return MBX_OK;
@@ -1626,7 +1644,7 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     ++stats_.kernel_launches;
     if (e != cudaSuccess) return fail_cuda("delta pass launch", e);
     cudaEventRecord(ev1_, st_);
-    cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    copy_async(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("delta pass", e);
@@ -1648,12 +1666,12 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     // Pending entries, arbitrary-precision recomputes and the next reference.
     hdone_.resize(n);
     hgmp_.resize(n);
-    cudaMemcpyAsync(hdone_.data(), ddone_.p, n, cudaMemcpyDeviceToHost, st_);
-    cudaMemcpyAsync(hgmp_.data(), dgmp_.p, n, cudaMemcpyDeviceToHost, st_);
+    copy_async(hdone_.data(), ddone_.p, n, cudaMemcpyDeviceToHost);
+    copy_async(hgmp_.data(), dgmp_.p, n, cudaMemcpyDeviceToHost);
     const bool glitches = !use_floatexp_;
     if (glitches) {
         hglitch_.resize(n);
-        cudaMemcpyAsync(hglitch_.data(), dglitch_.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st_);
+        copy_async(hglitch_.data(), dglitch_.p, sizeof(double) * n, cudaMemcpyDeviceToHost);
     }
     e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return fail_cuda("pass readback", e);
@@ -1729,8 +1747,8 @@ int Engine::recompute_gmp(const std::vector<int>& list, const std::function<void
     if (cancel_.load()) return MBX_E_CANCELLED;
     stats_.gmp_pixels += n;
     for (int q = 0; q < n; ++q) {
-        cudaMemcpyAsync(out_iter_ + idx[q], &vals[q], sizeof(float), cudaMemcpyHostToDevice, st_);
-        if (out_n_) cudaMemcpyAsync(out_n_ + idx[q], &ns[q], sizeof(int32_t), cudaMemcpyHostToDevice, st_);
+        copy_async(out_iter_ + idx[q], &vals[q], sizeof(float), cudaMemcpyHostToDevice);
+        if (out_n_) copy_async(out_n_ + idx[q], &ns[q], sizeof(int32_t), cudaMemcpyHostToDevice);
     }
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return fail_cuda("gmp writeback", e);
@@ -1739,8 +1757,8 @@ int Engine::recompute_gmp(const std::vector<int>& list, const std::function<void
 
 int Engine::write_sample(const int* a, float v, int32_t n) {
     const int idx = (a[0] * SUB_ + SUB_ / 2 + a[2]) * W_ * SUB_ + (a[1] * SUB_ + SUB_ / 2 + a[3]);
-    cudaMemcpyAsync(out_iter_ + idx, &v, sizeof(float), cudaMemcpyHostToDevice, st_);
-    if (out_n_) cudaMemcpyAsync(out_n_ + idx, &n, sizeof(int32_t), cudaMemcpyHostToDevice, st_);
+    copy_async(out_iter_ + idx, &v, sizeof(float), cudaMemcpyHostToDevice);
+    if (out_n_) copy_async(out_n_ + idx, &n, sizeof(int32_t), cudaMemcpyHostToDevice);
     return cuda_ok("sample write");
 }
 
@@ -1753,8 +1771,8 @@ int Engine::flush_ref_value() {
     ref_value_store_ = v;
     ref_n_store_ = n;
     const int idx = (ref_[0] * SUB_ + SUB_ / 2 + ref_[2]) * W_ * SUB_ + (ref_[1] * SUB_ + SUB_ / 2 + ref_[3]);
-    cudaMemcpyAsync(out_iter_ + idx, &ref_value_store_, sizeof(float), cudaMemcpyHostToDevice, st_);
-    if (out_n_) cudaMemcpyAsync(out_n_ + idx, &ref_n_store_, sizeof(int32_t), cudaMemcpyHostToDevice, st_);
+    copy_async(out_iter_ + idx, &ref_value_store_, sizeof(float), cudaMemcpyHostToDevice);
+    if (out_n_) copy_async(out_n_ + idx, &ref_n_store_, sizeof(int32_t), cudaMemcpyHostToDevice);
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return fail_cuda("reference value", e);
     return MBX_OK;
@@ -1846,9 +1864,9 @@ int Engine::batch_finish(const mbx_request& r, mbx_stats* out_stats) {
     const size_t nsamp = (size_t)r.width * r.height * r.sub * r.sub;
     const double t0 = now_ms();
     if (!r.outputs_on_device) {
-        cudaMemcpyAsync(r.iterations, out_iter_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
-        if (r.normal) cudaMemcpyAsync(r.normal, out_norm_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
-        if (r.escape_iteration) cudaMemcpyAsync(r.escape_iteration, out_n_, sizeof(int32_t) * nsamp, cudaMemcpyDeviceToHost, st_);
+        copy_async(r.iterations, out_iter_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost);
+        if (r.normal) copy_async(r.normal, out_norm_, sizeof(float) * nsamp, cudaMemcpyDeviceToHost);
+        if (r.escape_iteration) copy_async(r.escape_iteration, out_n_, sizeof(int32_t) * nsamp, cudaMemcpyDeviceToHost);
         cudaError_t e = cudaStreamSynchronize(st_);
         stats_.copy_ms += now_ms() - t0;
         if (e != cudaSuccess) return fail_cuda("output readback", e);
@@ -1950,9 +1968,9 @@ int Engine::compute_frame(const mbx_request& r) {
     if (batch_slot_ && batch_slot_->deferred) return rc; // passes and readback follow in the batch
     if (rc == MBX_OK && !r.outputs_on_device) {
         const double t0 = now_ms();
-        cudaMemcpyAsync(r.iterations, out_iter, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
-        if (r.normal) cudaMemcpyAsync(r.normal, out_norm, sizeof(float) * nsamp, cudaMemcpyDeviceToHost, st_);
-        if (r.escape_iteration) cudaMemcpyAsync(r.escape_iteration, out_n, sizeof(int32_t) * nsamp, cudaMemcpyDeviceToHost, st_);
+        copy_async(r.iterations, out_iter, sizeof(float) * nsamp, cudaMemcpyDeviceToHost);
+        if (r.normal) copy_async(r.normal, out_norm, sizeof(float) * nsamp, cudaMemcpyDeviceToHost);
+        if (r.escape_iteration) copy_async(r.escape_iteration, out_n, sizeof(int32_t) * nsamp, cudaMemcpyDeviceToHost);
         e = cudaStreamSynchronize(st_);
         stats_.copy_ms += now_ms() - t0;
         if (e != cudaSuccess) return fail_cuda("output readback", e);
@@ -2126,7 +2144,7 @@ int Engine::supersample(int ref_it) {
     ++stats_.kernel_launches;
     if (e != cudaSuccess) return fail_cuda("ss flags", e);
     std::vector<uint8_t> flags((size_t)W_ * H_);
-    cudaMemcpyAsync(flags.data(), dflags_.p, flags.size(), cudaMemcpyDeviceToHost, st_);
+    copy_async(flags.data(), dflags_.p, flags.size(), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return fail_cuda("ss flags", e);
     std::vector<uint64_t> samples;
@@ -2232,7 +2250,7 @@ int Engine::render_julia(mpf_ptr z_re, mpf_ptr z_im, mpf_ptr scale, const char* 
     ++stats_.kernel_launches;
     ++stats_.passes;
     if (e != cudaSuccess) return fail_cuda("julia launch", e);
-    cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    copy_async(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("julia pass", e);
@@ -2271,7 +2289,7 @@ int Engine::render_shallow(volatile float* progress) {
     ++stats_.kernel_launches;
     ++stats_.passes;
     if (e != cudaSuccess) return fail_cuda("shallow launch", e);
-    cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    copy_async(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("shallow pass", e);
@@ -2287,7 +2305,7 @@ int Engine::render_shallow(volatile float* progress) {
 int Engine::shallow_samples(const std::vector<uint64_t>& samples) {
     const int n = (int)samples.size();
     if (!ensure(dkeys_, n) || !ensure(ddone_, n)) return MBX_E_NOMEM;
-    cudaMemcpyAsync(dkeys_.p, samples.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st_);
+    copy_async(dkeys_.p, samples.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice);
     ShallowParams p;
     p.g = geom();
     p.g.deovl = 0; // sub-samples carry the smooth/EDE value only (mp.cpp:1936-1967)
@@ -2310,7 +2328,7 @@ int Engine::shallow_samples(const std::vector<uint64_t>& samples) {
     ++stats_.kernel_launches;
     ++stats_.passes;
     if (e != cudaSuccess) return fail_cuda("shallow ss launch", e);
-    cudaMemcpyAsync(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st_);
+    copy_async(hctr_, dctr_, sizeof(Counters), cudaMemcpyDeviceToHost);
     e = cudaStreamSynchronize(st_);
     stats_.kernel_ms += now_ms() - t0;
     if (e != cudaSuccess) return fail_cuda("shallow ss pass", e);

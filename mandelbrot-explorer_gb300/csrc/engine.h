@@ -141,6 +141,9 @@ class Engine {
     FrameGeom geom() const;
     int cuda_ok(const char* what);
     int fail_cuda(const char* what, cudaError_t e);
+    // cudaMemcpyAsync on the context's stream; host<->device bytes are counted
+    // into the frame's statistics (h2d_bytes / d2h_bytes)
+    cudaError_t copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind);
     void release_device();
     template <typename T>
     bool ensure(DevBuf<T>& b, size_t n);

@@ -116,7 +116,7 @@ struct Outputs {
 };
 
 struct Counters {
-    unsigned long long steps, bla_applies, bla_skipped, rebases, rescales;
+    unsigned long long steps, bla_applies, bla_skipped, rebases;
     unsigned int next;  // work-queue head
     unsigned int interior;
     unsigned long long glitch_min_bits;  // min glitch score (as non-negative double bits)
@@ -128,6 +128,10 @@ struct Counters {
     unsigned int probe_hit;              // interior gate probe: set by the first interior decision (the probe then stops)
     unsigned long long exact_steps;      // lane passes: steps taken in floatexp (orbit or delta below the lane's range)
     unsigned long long fe_rebases;       // lane passes: rebases decided in floatexp
+    // lane passes: blocks whose TMA orbit staging missed its wait limit (low 16
+    // bits; such a block reads the orbit from global memory) and, times 2^16,
+    // those whose copy was still in flight after a second bounded wait at exit
+    unsigned int stage_timeouts;
 };
 
 struct FrameGeom {

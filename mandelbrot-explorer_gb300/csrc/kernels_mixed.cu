@@ -56,6 +56,20 @@ __device__ __forceinline__ float tlog2(float x) { return log2f(x); }
 __device__ __forceinline__ double tlog2(double x) { return log2(x); }
 __device__ __forceinline__ float tlog2(df32 x) { return log2f(x.hi + x.lo); }
 
+// Bounded wait on phase 0 of an mbarrier: true once the phase completed, false
+// after `limit` polls.
+__device__ bool mbar_wait_bounded(unsigned mb, int limit) {
+    unsigned done = 0;
+    for (int spin = 0; spin < limit && !done; ++spin) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mb)
+            : "memory");
+    }
+    return done != 0;
+}
+
 // Stage the FP32 orbit into shared memory: bulk TMA copies (cp.async.bulk,
 // global -> shared) completing on one mbarrier; the wait is bounded.
 __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned long long* mbar) {
@@ -74,15 +88,7 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
         }
     }
     __syncthreads();
-    unsigned done = 0;
-    for (int spin = 0; spin < (1 << 22) && !done; ++spin) {
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(mb)
-            : "memory");
-    }
-    return done != 0;
+    return mbar_wait_bounded(mb, 1 << 22);
 }
 
 // Iterations a lane takes per lane_run call between the warp's refill points.
@@ -114,16 +120,21 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     // to the lower blocks), before any orbit staging.
     if ((long long)blockIdx.x * (MAXT / 32) * LANES >= n) return;
     const unsigned take = LANES == 32 ? 0xffffffffu : ((1u << LANES) - 1u);
+    bool stage_late = false;
     if (LaneReal<T>::kTrackError && p.orbit_in_smem) {
         V2* so = reinterpret_cast<V2*>(smem_raw);
         bool ok = stage_orbit(reinterpret_cast<float2*>(so), reinterpret_cast<const float2*>(orbit), p.smem_entries * (int)(sizeof(V2) / sizeof(float2)), &mbar);
         if (threadIdx.x == 0) stage_ok = ok ? 1 : 0;
         __syncthreads();
-        if (!stage_ok) {
-            if (threadIdx.x == 0) atomicAdd(&f.ctr->rescales, 1ull); // staging timed out: this block leaves its share to the others
-            return;
+        if (stage_ok) {
+            orb = so;
+        } else {
+            // the copy did not complete within the wait limit: this block reads
+            // the orbit from global memory instead, and waits for the copy
+            // again (bounded) before it exits, so that no copy outlives it
+            stage_late = true;
+            if (threadIdx.x == 0) atomicAdd(&f.ctr->stage_timeouts, 1u);
         }
-        orb = so;
     }
     const int reflen = p.mx_ref_it + 1;
     const T ESC2f = (T)g.ESC2;
@@ -219,6 +230,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     atomicAdd(&f.ctr->finished, n_fin);
     if (n_intflag) atomicAdd(&f.ctr->interior_flagged, n_intflag);
     atomicAdd(&f.ctr->interior, n_int);
+    if (stage_late && !mbar_wait_bounded((unsigned)__cvta_generic_to_shared(&mbar), 1 << 24) && threadIdx.x == 0) atomicAdd(&f.ctr->stage_timeouts, 1u << 16);
 }
 
 // ---- batched passes over several views ------------------------------------
@@ -440,8 +452,8 @@ int Engine::prepare_mixed() {
         }
         for (size_t k = 0; k < hdpxy_.size(); ++k) hdpxyf_[k] = (float)hdpxy_[k];
         if (!ensure(ddpxy_, hdpxy_.size()) || !ensure(ddpxyf_, hdpxyf_.size())) return MBX_E_NOMEM;
-        cudaMemcpyAsync(ddpxy_.p, hdpxy_.data(), sizeof(double) * hdpxy_.size(), cudaMemcpyHostToDevice, st_);
-        cudaMemcpyAsync(ddpxyf_.p, hdpxyf_.data(), sizeof(float) * hdpxyf_.size(), cudaMemcpyHostToDevice, st_);
+        copy_async(ddpxy_.p, hdpxy_.data(), sizeof(double) * hdpxy_.size(), cudaMemcpyHostToDevice);
+        copy_async(ddpxyf_.p, hdpxyf_.data(), sizeof(float) * hdpxyf_.size(), cudaMemcpyHostToDevice);
         dpxy_w_ = nx;
     }
     if (!ensure(dZf_, (size_t)len + 4) || !ensure(dZdf_, (size_t)len + 4)) return MBX_E_NOMEM;

@@ -19,6 +19,7 @@ constexpr int kNoAllocMaxSamples = 1 << 21; // 2,097,152 samples (1920x1080 fits
 // Scratch: Counters followed by one completion byte per sample. Every GPU that
 // loads this library holds this array until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[256 + kNoAllocMaxSamples];
+static_assert(sizeof(Counters) <= 256, "the counters must fit the scratch array's 256-byte header");
 
 std::mutex g_setup_mu;
 void* g_scratch_addr[64] = {nullptr};
@@ -30,6 +31,8 @@ extern "C" int mbx_render_shallow_noalloc(double c0_re, double c0_im, double dx,
     using namespace mbx;
     if (width < 2 || height < 2 || max_iterations < 1 || !iterations) return MBX_E_INVALID;
     if ((coloring_method & ~(MBX_EXTERIOR_DIST_EST | MBX_DE_OVERLAY)) != 0) return MBX_E_INVALID;
+    // the distance overlay is written to the normal buffer: without one it has nowhere to go
+    if ((coloring_method & MBX_DE_OVERLAY) && !normal) return MBX_E_INVALID;
     if ((long long)width * height > kNoAllocMaxSamples) return MBX_E_TOO_LARGE;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MBX_E_NODEVICE;
@@ -57,7 +60,7 @@ extern "C" int mbx_render_shallow_noalloc(double c0_re, double c0_im, double dx,
     if (cudaMemsetAsync(ctr, 0, sizeof(Counters), st) != cudaSuccess) return MBX_E_CUDA;
     if (launch_fill(iterations, normal, escape_iteration, n, st) != cudaSuccess) return MBX_E_CUDA;
     const float escf = (float)(bailout > 0 ? bailout : 1e8);
-    ShallowParams p;
+    ShallowParams p{}; // value-initialised: fields not set below (normal map off) are zero
     p.g.W = width;
     p.g.H = height;
     p.g.sub = 1;

@@ -113,6 +113,11 @@ class Stats(ctypes.Structure):
         ("exact_steps", ctypes.c_longlong),
         ("fe_rebases", ctypes.c_longlong),
         ("exact_reruns", ctypes.c_longlong),
+        ("h2d_bytes", ctypes.c_longlong),
+        ("d2h_bytes", ctypes.c_longlong),
+        ("fp32_pass_gpu_ms", ctypes.c_double),
+        ("fp32_pass_steps", ctypes.c_longlong),
+        ("fp32_pass_bla_applies", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -80,6 +80,17 @@ def c2_views(seed: int = 2, width: int = 1920, height: int = 1080, max_iteration
     return [deep_view(k, seed, width, height, max_iterations) for k in (300, 1000)]
 
 
+# Frames with committed arbitrary-precision truth subsets (tests/golden/make_truth.py).
+TRUTH_FRAMES = ("1e-300", "1e-1000")
+
+
+def frame(label: str, width: int = 1920, height: int = 1080):
+    """A benchmark frame by label."""
+    if label in ("1e-300", "1e-1000"):
+        return deep_view(int(label[3:]), width=width, height=height)
+    raise KeyError(label)
+
+
 if __name__ == "__main__":
     import sys
 

@@ -13,7 +13,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "lib", "libmbx_oracle.so")
-REFERENCE = "/root/reference"
+# Where the reference project's sources lie (read-only); override with MBX_REFERENCE_DIR.
+REFERENCE = os.environ.get("MBX_REFERENCE_DIR", "/root/reference")
 
 
 def find_libgmp():

@@ -69,3 +69,13 @@ def load_julia_cases():
 def load_julia_fixture(name):
     """The reference engine's Mandel::ComputeJulia output for a case (float32)."""
     return np.fromfile(os.path.join(GOLDEN, "ref_julia_%s.f32" % name), dtype="<f4")
+
+
+def load_truth(label):
+    """(idx, N, value) of a 1080p frame's committed arbitrary-precision truth
+    subset (tests/golden/make_truth.py), or None when it has not been made."""
+    p = os.path.join(GOLDEN, "truth_c2_%s.npz" % label)
+    if not os.path.exists(p):
+        return None
+    z = np.load(p)
+    return z["idx"], z["N"], z["value"]

@@ -23,7 +23,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+# The reference project's sources (read-only); override with MBX_REFERENCE_DIR.
+REF = os.environ.get("MBX_REFERENCE_DIR", "/root/reference")
 DUMP = os.path.join(ROOT, "oracle", "_ref", "mbx_refdump")
 TRUTH = {
     "point31": "point_7e31.f32",

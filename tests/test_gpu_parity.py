@@ -60,6 +60,24 @@ def test_exact_matches_reference_fixture(backend, name):
         np.testing.assert_allclose(nr, ref_nr, rtol=RTOL, atol=0)
 
 
+def test_c1_config_matches_oracle(backend):
+    """The plain FP64 configuration as stated: the seahorse-valley centre
+    extended to 120 seed-drawn digits, 1280x720, half-width 1e-30, maxiter
+    50000, bailout 2^8, through mbx_compute in the exact form against the
+    oracle's restatement of the reference's double delta loop
+    (mp.cpp:2290-2585): class and N identical at every sample, value within
+    1e-6 relative."""
+    import views
+
+    v = views.c1_view()
+    c = dict(v, width=1280, height=720, sub=1, coloring_method=0)
+    it, _, en, st = gpu_render(backend, c, precision_mode=mbx.PRECISION_EXACT)
+    assert st["used_floatexp"] == 0  # scale 2e30 stays on the double path
+    oit, _, oen, _ = oracle.render(v["center_re"], v["center_im"], v["scale"], 1280, 720, v["max_iterations"], bailout=v["bailout"])
+    assert_same(it, en, oit, oen, "c1 1280x720")
+    print("\n[c1 1280x720] %d samples identical in class and N; N %d..%d" % (en.size, int(en[en > 0].min(initial=0)), int(en.max())))
+
+
 def test_repeat_is_deterministic(backend):
     c = CASES["flake"]
     a = gpu_render(backend, c)[0]

@@ -93,3 +93,24 @@ def test_oracle_julia_matches_reference_build(name):
         assert np.array_equal(ref.view(np.uint32), it.view(np.uint32)), "oracle differs from the reference build"
     else:
         np.testing.assert_allclose(it, ref, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("label", ["1e-300", "1e-1000"])
+def test_truth_subsets_reproduce(label):
+    """The committed arbitrary-precision truth subsets of the 1080p deep frames
+    (tests/golden/make_truth.py) are what the oracle's per-sample GMP iteration
+    gives: a few of their samples recomputed, N exact, value within 1e-6."""
+    import views
+    from conftest import load_truth
+
+    tr = load_truth(label)
+    if tr is None:
+        pytest.skip("truth subset not made")
+    idx, tn, tv = tr
+    assert idx.size == 4096 and np.all(np.diff(idx) > 0)
+    pick = np.arange(0, idx.size, idx.size // 6)[:6]
+    v = views.frame(label)
+    keys = np.stack([idx[pick] // 1920, idx[pick] % 1920, np.zeros(pick.size, int), np.zeros(pick.size, int)], axis=1)
+    got_v, got_n = oracle.truth(v["center_re"], v["center_im"], v["scale"], 1920, 1080, v["max_iterations"], keys, bailout=v["bailout"])
+    assert np.array_equal(got_n, tn[pick])
+    np.testing.assert_allclose(got_v, tv[pick], rtol=1e-6, atol=0)

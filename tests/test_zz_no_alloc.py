@@ -36,7 +36,10 @@ def test_noalloc_matches_regular_entry_point():
     # half-height 65/64, dx = 2*(2/127) (mpf-truncated then truncated to a
     # double), dy = 2*(65/64)/64 (exact).
     W, H, mxit = 128, 65, 3000
-    for cm in (0, mbx.EXTERIOR_DIST_EST):
+    # plain smooth values, exterior distance, and the distance overlay (the one
+    # colouring that writes the second buffer; it takes the scalar loop)
+    for cm in (0, mbx.EXTERIOR_DIST_EST, mbx.DE_OVERLAY):
+        overlay = bool(cm & mbx.DE_OVERLAY)
         be = mbx.create_compute_backend("cuda")
         req = mbx.ComputeRequest("-0.5", "0", "1", W, H, mxit, coloring_method=cm, bailout=1e8)
         assert be.compute_status(req) == mbx.OK, be.last_error()
@@ -47,15 +50,31 @@ def test_noalloc_matches_regular_entry_point():
         lib = mbx.load_library()
         it = torch.empty(W * H, dtype=torch.float32, device="cuda")
         en = torch.empty(W * H, dtype=torch.int32, device="cuda")
+        nr = torch.empty(W * H, dtype=torch.float32, device="cuda") if overlay else None
         for call in range(2):
             it.fill_(123.0)
             en.fill_(7)
-            rc = lib.mbx_render_shallow_noalloc(c0r, c0i, dx, dy, W, H, mxit, 1e8, cm, ctypes.c_void_p(it.data_ptr()), ctypes.c_void_p(en.data_ptr()), None, None)
-            assert rc == mbx.OK, "call %d returned %d" % (call, rc)
+            if nr is not None:
+                nr.fill_(55.0)
+            rc = lib.mbx_render_shallow_noalloc(c0r, c0i, dx, dy, W, H, mxit, 1e8, cm, ctypes.c_void_p(it.data_ptr()), ctypes.c_void_p(en.data_ptr()),
+                                                ctypes.c_void_p(nr.data_ptr()) if nr is not None else None, None)
+            assert rc == mbx.OK, "cm %d call %d returned %d" % (cm, call, rc)
             got_it = it.cpu().numpy()
             got_en = en.cpu().numpy()
-            assert np.array_equal(got_it.view(np.uint32), req.iterations.view(np.uint32)), "call %d: values differ" % call
-            assert np.array_equal(got_en, req.escape_iteration), "call %d: escape iterations differ" % call
+            assert np.array_equal(got_it.view(np.uint32), req.iterations.view(np.uint32)), "cm %d call %d: values differ" % (cm, call)
+            assert np.array_equal(got_en, req.escape_iteration), "cm %d call %d: escape iterations differ" % (cm, call)
+            if overlay:
+                got_nr = nr.cpu().numpy()
+                assert np.array_equal(got_nr.view(np.uint32), req.normal.view(np.uint32)), "call %d: overlay distances differ" % call
+
+
+def test_noalloc_overlay_needs_its_buffer():
+    """The distance overlay goes to the normal buffer: without one the call is rejected."""
+    torch = pytest.importorskip("torch")
+    lib = mbx.load_library()
+    it = torch.empty(16 * 16, dtype=torch.float32, device="cuda")
+    rc = lib.mbx_render_shallow_noalloc(-2.5, -1.0, 0.2, 0.1, 16, 16, 100, 1e8, mbx.DE_OVERLAY, ctypes.c_void_p(it.data_ptr()), None, None, None)
+    assert rc == mbx.E_INVALID
 
 
 def test_noalloc_rejects_oversized_frames():
