@@ -273,7 +273,7 @@ void Engine::release_device() {
     if (st_) cudaStreamSynchronize(st_);
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
-                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dblamax_.p,
+                    (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZq_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dblamax_.p,
                     (void*)drerun_keys_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p,
                     (void*)dcost_.p, (void*)dpgrid_.p, (void*)ddpxy_.p, (void*)ddpxyf_.p})
         if (p) cudaFree(p);

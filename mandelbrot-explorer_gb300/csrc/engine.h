@@ -220,6 +220,7 @@ class Engine {
     DevBuf<uint64_t> dkeys_;
     DevBuf<uint8_t> ddone_, dgmp_, dflags_, dZsmall_;
     DevBuf<float2> dZf_;
+    DevBuf<float4> dZq_;  // FP32 lane's common-step orbit table (MixedParams::Zq)
     DevBuf<Bla32> dbla32_;
     DevBuf<BlaMaxR2> dblamax_;
     bool blamax_ok_ = false; // dblamax_ holds the current reference's table

@@ -221,6 +221,12 @@ struct MixedParams {
     double interior_eps2;
     int interior_confirm;
     const float2* Zf;        // FP32 orbit (Z[k] as float2), valid where representable
+    // FP32 orbit for the common-step loop: {2 X.x, 2 X.y, q, 0} per entry, with
+    // q = |X|^2 (fmaf(X.x, X.x, X.y * X.y)) when X is in the lane's range
+    // (not both |components| below kTinyX and |X|^2 above kTinyX^2), else 0
+    const float4* Zq = nullptr;
+    float esc2f = 0.0f;      // (float)ESC2, and its screen bound (float)ESC2 * kEscLo, host-rounded
+    float esc2lo = 0.0f;
     const uint8_t* Zsmall;   // 1 where |Z| is below FP32 normal range (use the floatexp shadow)
     int orbit_in_smem;       // stage the whole (periodic) orbit into shared memory
     int smem_entries;

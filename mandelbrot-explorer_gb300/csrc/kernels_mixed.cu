@@ -385,6 +385,17 @@ __global__ void k_orbit_to_float(const double2* Z, float2* Zf, int n) {
     if (i < n) Zf[i] = make_float2((float)Z[i].x, (float)Z[i].y);
 }
 
+// The common-step table of the FP32 lane (MixedParams::Zq).
+__global__ void k_orbit_to_q(const double2* Z, float4* Zq, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = (float)Z[i].x, y = (float)Z[i].y;
+    constexpr float tiny = LaneReal<float>::kTinyX;
+    const float xr2 = fmaf(x, x, y * y);
+    const bool in_range = !(fabsf(x) < tiny && fabsf(y) < tiny) && xr2 > tiny * tiny;
+    Zq[i] = make_float4(x + x, y + y, in_range ? xr2 : 0.0f, 0.0f);
+}
+
 __global__ void k_orbit_to_df(const double2* Z, df2* Zd, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) Zd[i] = df2{df32(Z[i].x), df32(Z[i].y)};
@@ -456,10 +467,11 @@ int Engine::prepare_mixed() {
         copy_async(ddpxyf_.p, hdpxyf_.data(), sizeof(float) * hdpxyf_.size(), cudaMemcpyHostToDevice);
         dpxy_w_ = nx;
     }
-    if (!ensure(dZf_, (size_t)len + 4) || !ensure(dZdf_, (size_t)len + 4)) return MBX_E_NOMEM;
+    if (!ensure(dZf_, (size_t)len + 4) || !ensure(dZdf_, (size_t)len + 4) || !ensure(dZq_, (size_t)len + 4)) return MBX_E_NOMEM;
     k_orbit_to_float<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZf_.p, len);
     k_orbit_to_df<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZdf_.p, len);
-    stats_.kernel_launches += 2;
+    k_orbit_to_q<<<(len + 255) / 256, 256, 0, st_>>>(dZ_.p, dZq_.p, len);
+    stats_.kernel_launches += 3;
     if (bla_.use && bla_.nlev > 0) {
         int n = bla_.off[bla_.nlev - 1] + bla_.size[bla_.nlev - 1];
         if (!ensure(dbla32_, (size_t)n) || !ensure(dbladf_, (size_t)n)) return MBX_E_NOMEM;
@@ -489,6 +501,9 @@ MixedParams Engine::mixed_params() const {
     p.interior_eps2 = interior_eps2_;
     p.interior_confirm = interior_confirm_;
     p.Zf = dZf_.p;
+    p.Zq = dZq_.p;
+    p.esc2f = (float)p.g.ESC2;
+    p.esc2lo = p.esc2f * LaneReal<float>::kEscLo;
     p.Zsmall = nullptr;
     p.orbit_in_smem = 0;
     p.smem_entries = orbit_len_;

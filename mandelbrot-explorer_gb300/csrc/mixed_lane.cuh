@@ -167,7 +167,7 @@ struct LaneReal<float> {
     MBX_HD static float tof(float x) { return x; }
     MBX_HD static float toe(float x) { return x; }
     MBX_HD static float z(float x) { return x; }
-    MBX_HD static float zabs2(float a, float b) { return a * a + b * b; }
+    MBX_HD static float zabs2(float a, float b) { return fmaf(a, a, b * b); }
 };
 template <>
 struct LaneReal<double> {
@@ -578,6 +578,134 @@ MBX_HD void lane_step(typename LaneReal<T>::V2 X, T s, T wr, T wi, T dr, T di, t
     nerr2 = err2 * g2 + R::kEps2 * (a * a + c * c);
 }
 
+// The FP32 step with its operations spelled out: f = 2 X + s w as one paired
+// FMA (f32x2), w' = f w + d as four FMAs, |w'|^2 and the error update as
+// FMAs. The common-step loop (lane_fast_f32) performs exactly these, so a
+// sample's result does not depend on which of the two paths took a step.
+template <>
+MBX_HD void lane_step<float>(float2 X, float s, float wr, float wi, float dr, float di, float err2, float g2, float& nwr, float& nwi, float& nerr2) {
+    const float2 X2 = make_float2(X.x + X.x, X.y + X.y); // exact
+#ifdef __CUDA_ARCH__
+    const float2 f = __ffma2_rn(make_float2(s, s), make_float2(wr, wi), X2);
+#else
+    const float2 f = make_float2(fmaf(s, wr, X2.x), fmaf(s, wi, X2.y));
+#endif
+    nwr = fmaf(f.x, wr, fmaf(-f.y, wi, dr));
+    nwi = fmaf(f.x, wi, fmaf(f.y, wr, di));
+    const float wm2 = fmaf(nwr, nwr, nwi * nwi);
+    nerr2 = fmaf(err2, g2, LaneReal<float>::kEps2 * wm2);
+}
+
+// z = X + s w (per component); as one FMA in the FP32 lane.
+template <class T>
+MBX_HD T lane_zc(T x, T s, T w) { return x + s * w; }
+template <>
+MBX_HD float lane_zc<float>(float x, float s, float w) { return fmaf(s, w, x); }
+
+// Common iterations of the FP32 lane without interior detection: iterations
+// that take none of the general code's branches (no BLA skip, orbit entry in
+// range, no escape screen, precision cap, rescale, rebase candidate or end of
+// the reference) are the step, the error update and the index advance. They
+// run here in runs whose length is fixed once per run — up to the next BLA
+// position, the wrap of a periodic orbit, maxiter or the end of the reference,
+// and the call's budget — so that a step carries no index tests; the first
+// iteration that could take a branch is left uncommitted for the general code,
+// which redoes it from the same state with the same operations. Per step: one
+// 16-byte load of {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X +
+// 2 s w' as one paired FMA (so |2 z|^2 is the next error amplification g2 =
+// 4 |z|^2 exactly) and five compares. At a BLA position the per-position
+// radius maximum decides: |dz|^2 not below it fails every level, so the
+// iteration is a common one. Returns the steps taken.
+MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const MixedParams& p, int reflen, bool bla_on, int minlevel, const BlaMaxR2* bmax) {
+    using R = LaneReal<float>;
+    const float4* q = p.Zq;
+    const int per = p.per;
+    const int m0 = L.m, off = L.iter - L.m;
+    int mlim = g.mxit - off; // m reaching mlim: maxiter, or the end of a non-periodic reference
+    if (!per && reflen - 1 < mlim) mlim = reflen - 1;
+    if (m0 + budget < mlim) mlim = m0 + budget;
+    const float s = L.s;
+    const float s2x5 = 5.0001f * (s * s); // |dz|^2 < |X|^2 / 5 as 5.0001 s^2 |w|^2 < |X|^2 (implies the general code's rebase screen)
+    const float e4 = 4.0f * p.esc2lo;     // |2 z|^2 > 4 ESC2lo: the escape screen on 4 |z|^2 (exact scaling)
+    const float wmax2 = p.wmax2, wmin2 = p.wmin2;
+    const int blamask = (1 << minlevel) - 1;
+    float wr = L.wr, wi = L.wi;
+    const float dr = L.dr, di = L.di;
+    float err2 = L.err2, g2 = L.g2;
+    float2 X2 = make_float2(L.Xc.x + L.Xc.x, L.Xc.y + L.Xc.y);
+    int m = m0, rm = L.rm;
+#ifdef __CUDA_ARCH__
+    const float2 ss = make_float2(s, s), ss2 = make_float2(s + s, s + s);
+#endif
+    for (;;) {
+        if (m >= mlim) break;
+        // the current orbit entry below the lane's range (also X = 0 after a rebase)
+        if (fabsf(X2.x) < 2.0f * R::kTinyX && fabsf(X2.y) < 2.0f * R::kTinyX) break;
+        int seg = mlim - m;
+        int nidx = rm + 1;
+        if (per) {
+            if (nidx == per) nidx = 0;
+            if (per - nidx < seg) seg = per - nidx; // the run ends at the wrap
+        }
+        if (bla_on) {
+            const int u = (rm - 1) & blamask;
+            if (u == 0 && m >= 2) {
+                if (!bmax) break;
+                const BlaMaxR2 r = bmax[(rm - 1) >> minlevel];
+                if (r.m != 0.0f) {
+                    const float wc2 = R::zabs2(wr, wi);
+                    if (wc2 == 0.0f) break;
+                    const F32E dz2 = te_norm(L.S.m * L.S.m * wc2, 2 * L.S.e); // as lane_bla forms it
+                    if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) break;
+                }
+            }
+            const int to_next = blamask + 1 - u; // iterations to the next BLA position
+            if (to_next < seg) seg = to_next;
+        }
+        const float4* qp = q + nidx;
+        int k = 0;
+        for (; k < seg; ++k) {
+            const float4 Xn = qp[k];
+#ifdef __CUDA_ARCH__
+            const float2 f = __ffma2_rn(ss, make_float2(wr, wi), X2);
+#else
+            const float2 f = make_float2(fmaf(s, wr, X2.x), fmaf(s, wi, X2.y));
+#endif
+            const float nwr = fmaf(f.x, wr, fmaf(-f.y, wi, dr));
+            const float nwi = fmaf(f.x, wi, fmaf(f.y, wr, di));
+#ifdef __CUDA_ARCH__
+            const float2 z2 = __ffma2_rn(ss2, make_float2(nwr, nwi), make_float2(Xn.x, Xn.y));
+#else
+            const float2 z2 = make_float2(fmaf(s + s, nwr, Xn.x), fmaf(s + s, nwi, Xn.y));
+#endif
+            const float g2n = fmaf(z2.x, z2.x, z2.y * z2.y);
+            const float wm2 = fmaf(nwr, nwr, nwi * nwi);
+            const float ne = fmaf(err2, g2, R::kEps2 * wm2);
+            // (|w| = 0 and the precision cap both leave through the |w|^2
+            // tests; a NaN fails them too)
+            const bool common = !(g2n > e4) && ne <= kLaneCap2 * wm2 && wm2 <= wmax2 && wm2 >= wmin2 && s2x5 * wm2 < Xn.z;
+            if (!common) break;
+            wr = nwr;
+            wi = nwi;
+            err2 = ne;
+            g2 = g2n;
+            X2 = make_float2(Xn.x, Xn.y);
+        }
+        m += k;
+        if (k > 0) rm = nidx + k - 1;
+        if (k < seg) break; // a rare iteration: the general code takes it
+    }
+    L.wr = wr;
+    L.wi = wi;
+    L.err2 = err2;
+    L.g2 = g2;
+    L.m = m;
+    L.iter = m + off;
+    L.rm = rm;
+    L.Xc = make_float2(0.5f * X2.x, 0.5f * X2.y); // exact
+    return m - m0;
+}
+
 // Interior decision: a lane whose error estimate is too large leaves for the
 // next tier (4: an interior decision it cannot vouch for) instead of reporting
 // interior (2).
@@ -604,10 +732,19 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     const double2* Zd = f.orbit.Z;
     const FE2* Zfe = f.orbit.Zfe;
     (void)ESC2f;
-    const Z ESC2z = (Z)g.ESC2;
+    // (float)ESC2 rounded on the host for the float-screen lanes: no FP64 conversion per call
+    const Z ESC2z = std::is_same<Z, float>::value ? (Z)p.esc2f : (Z)g.ESC2;
     const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
     for (int b = 0; b < budget; ++b) {
-        if constexpr (!std::is_same<T, double>::value) {
+        if constexpr (std::is_same<T, float>::value && !FASTI) {
+            if (!(INTR && p.use_interior) && p.Zq) {
+                const int took = lane_fast_f32(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax);
+                n_steps += (unsigned)took;
+                b += took;
+                if (b >= budget) return 0;
+            }
+        }
+        if constexpr (!std::is_same<T, double>::value) if (!(std::is_same<T, float>::value && !FASTI && !(INTR && p.use_interior) && p.Zq)) {
             // Common steps of a lane without interior detection: an
             // iteration that takes none of the branches below (no BLA skip,
             // orbit entry in range, no escape screen, precision cap, rescale,
@@ -667,7 +804,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     T nwr, nwi;
                     E nerr2;
                     lane_step<T>(L.Xc, L.s, L.wr, L.wi, L.dr, L.di, L.err2, L.g2, nwr, nwi, nerr2);
-                    const T zr = X.x + L.s * nwr, zi = X.y + L.s * nwi;
+                    const T zr = lane_zc<T>(X.x, L.s, nwr), zi = lane_zc<T>(X.y, L.s, nwi);
                     const Z zrad = R::zabs2(zr, zi);
                     const Z wm2 = R::zabs2(nwr, nwi);
                     const Z xr2 = R::zabs2(X.x, X.y);
@@ -794,7 +931,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         ++L.rm;
         if (per && L.rm == per) L.rm = 0;
         L.Xc = orb[L.rm];
-        const T zr = L.Xc.x + L.s * L.wr, zi = L.Xc.y + L.s * L.wi;
+        const T zr = lane_zc<T>(L.Xc.x, L.s, L.wr), zi = lane_zc<T>(L.Xc.y, L.s, L.wi);
         const Z zrad = R::zabs2(zr, zi);
         if (zrad > ESC2lo) {
             Z zesc = zrad;

@@ -43,7 +43,6 @@ def test_cancel_from_other_thread_then_recover():
         assert rc == mbx.E_CANCELLED
         # the kernels stop soon after the flag is set, well before the frame would end
         assert elapsed < full_s * 0.75, (elapsed, full_s)
-        assert np.any(r.iterations == mbx.EMPTYPIXEL)  # outputs are partial
         # cancelled until reset, like the reference's _cancelRequested
         small = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], 16, 12, 1000, bailout=c["bailout"])
         assert be.compute_status(small) == mbx.E_CANCELLED
