@@ -2,10 +2,14 @@
 FP64 GPU form, at accuracy, with the reference path's CPU restatement timed on
 the host cores beside them.
 
-Workload (one step): the two precision frames — 1920x1080, maxiter 1e6,
-bailout 2^8, half-widths 1e-300 and 1e-1000, centred a seed-drawn 1e-(k+5)
-vector from the Newton-refined period-14164 nucleus (views.c2_views). Inputs are
-synthetic seeded views; the reference publishes no dataset.
+Workload (one step): three 1920x1080 frames at maxiter 1e6, bailout 2^8 — the
+two precision frames, half-widths 1e-300 and 1e-1000 centred a seed-drawn
+1e-(k+5) vector from the Newton-refined period-14164 nucleus (views.c2_views;
+read literally, the first is all exterior and the second all interior), and a
+1e-1000 frame holding a whole period-1331 minibrot with its surroundings
+(views.minibrot_view: exterior escape iterations ~14,500 to ~575,000, 8 %
+interior). Inputs are synthetic seeded views; the reference publishes no
+dataset.
 
   value  : effective pixel-iterations (sum of N, maxiter for interior) per second
            of the tuned form through the C ABI with device-resident outputs and
@@ -165,7 +169,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--cpu-sample", default="1920x1080", help="cpu_baseline sample size (same views); one render of each")
+    ap.add_argument("--cpu-sample", default="960x540", help="cpu_baseline sample size (same views); one render of each")
     ap.add_argument("--ref-sample", default="960x540", help="--impl reference per-step sample size (same views)")
     ap.add_argument("--plain-sample", default="full", help="plain FP64 GPU sample size (same views), WxH or 'full' (the frames' own size)")
     ap.add_argument("--profile", default=None, help="comma-separated view labels (e.g. 1e-300): render (and colour) only those, default launch shape, no baselines (for ncu captures)")
@@ -174,7 +178,7 @@ def main():
     rank, world, local = dist_env()
     import views
 
-    vlist = views.c2_views(width=args.width, height=args.height)
+    vlist = views.c2_views(width=args.width, height=args.height) + [views.minibrot_view(width=args.width, height=args.height)]
     sw, sh = (int(x) for x in args.cpu_sample.split("x"))
     threads = os.cpu_count() or 1
 
@@ -210,8 +214,8 @@ def main():
             "vs_baseline": None,
             "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "C2 deep frames 1e-300 + 1e-1000, sampled at %dx%d of the 1920x1080 view" % (sw, sh), "maxiter": 1000000, "bailout": 256},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": "both C2 views rendered at %dx%d (same view region) per step by the oracle (CPU restatement of the reference path; the reference's AVX2 sources do not build on this Arm host)" % (sw, sh)},
+            "config": {"workload": "1080p deep frames 1e-300, 1e-1000 and 1e-1000 with a minibrot, sampled at %dx%d of the 1920x1080 views" % (sw, sh), "maxiter": 1000000, "bailout": 256},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": "the three views rendered at %dx%d (same view regions) per step by the oracle (CPU restatement of the reference path; the reference's AVX2 sources do not build on this Arm host)" % (sw, sh)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
@@ -299,7 +303,7 @@ def main():
     ms_per_step = elapsed / args.steps * 1e3
     value = tot[0] * world / elapsed / 1e9
 
-    # the same frames through the batched API: both frames' passes in shared
+    # the same frames through the batched API: the frames' passes in shared
     # launches (one CUDA graph), references resident
     bat = mbx.create_compute_backend("cuda", local)
     breqs = [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], W, H, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED,
@@ -316,7 +320,7 @@ def main():
     torch.cuda.synchronize()
     b_elapsed = time.perf_counter() - t0
     batched = {"ms_per_step": b_elapsed / args.steps * 1e3, "value": b_eff / b_elapsed / 1e9, "unit": UNIT, "shared_passes_gpu_ms": b_gpu / args.steps,
-               "note": "mbx_compute_batch: one CUDA graph per step holding both frames' probe, main and rerun passes; default launch shape"}
+               "note": "mbx_compute_batch: one CUDA graph per step holding the frames' probe, main and rerun passes; default launch shape"}
     # the learned-scheduled form: the cost model trains on the warm-up batches
     # (mode 1), then orders the timed ones (mode 2); outputs are identical
     ref_out = [o[1].clone() for o in outs]
@@ -333,19 +337,19 @@ def main():
     l_elapsed = time.perf_counter() - t0
     identical = all(bool(torch.equal(a, o[1])) for a, o in zip(ref_out, outs))
     batched["learned_order"] = {"ms_per_step": l_elapsed / args.steps * 1e3, "shared_passes_gpu_ms": l_gpu / args.steps, "identical_to_natural_order": identical}
-    # the 1e-1000 frame alone in the learned-scheduled form (the stated target
-    # compares it with the plain FP64 form)
-    deep = [q for q, v in zip(breqs, vlist) if v["label"] == "1e-1000"]
-    if deep:
+    # each 1e-1000 frame alone in the learned-scheduled form (the stated target
+    # compares a 1080p 1e-1000 frame in that form with the plain FP64 form)
+    batched["learned_order"]["frame_ms"] = {}
+    for q, v in zip(breqs, vlist):
+        if not v["label"].startswith("1e-1000"):
+            continue
         for _ in range(3):
-            assert bat.compute_batch(deep) == mbx.OK, bat.last_error()
-        d_gpu = 0.0
+            assert bat.compute_batch([q]) == mbx.OK, bat.last_error()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            assert bat.compute_batch(deep) == mbx.OK, bat.last_error()
-            d_gpu += bat.last_batch_stats.pass_gpu_ms
+            assert bat.compute_batch([q]) == mbx.OK, bat.last_error()
         torch.cuda.synchronize()
-        batched["learned_order"]["frame_1e-1000_ms"] = (time.perf_counter() - t0) / args.steps * 1e3
+        batched["learned_order"]["frame_ms"][v["label"]] = (time.perf_counter() - t0) / args.steps * 1e3
     bat.close()
 
     # image epilogue: the render tool's colouring (palette, gamma; ss 1) of each
@@ -384,9 +388,9 @@ def main():
         e2e_eff += st["effective_iterations"]
         host_frames.append(req.escape_iteration.copy())
     e2e_value = e2e_eff / e2e_t / 1e9
-    # the same step (both frames) as one mbx_compute_batch call with host
+    # the same step (all frames) as one mbx_compute_batch call with host
     # buffers and fresh references: the frames' GMP work runs concurrently on
-    # the host, their passes share one graph; D2H of both frames inside
+    # the host, their passes share one graph; D2H of every frame inside
     bat2 = mbx.create_compute_backend("cuda", local)
     b_reqs = [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], W, H, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED) for v in vlist]
     assert bat2.compute_batch(b_reqs) == mbx.OK, bat2.last_error()  # allocations
@@ -468,7 +472,7 @@ def main():
     if rank == 0:
         sw_, sh_ = sw, sh
         cpu_v, cpu_dt, cpu_eff = cpu_reference(vlist, sw_, sh_, threads)
-        cpu = {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": "both C2 views at %dx%d (same view region; %.1f s, %.3g pixel-iterations) by the oracle, the CPU restatement of the reference path" % (sw_, sh_, cpu_dt, cpu_eff)}
+        cpu = {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port", "sample": "the three views at %dx%d (same view regions; %.1f s, %.3g pixel-iterations) by the oracle, the CPU restatement of the reference path" % (sw_, sh_, cpu_dt, cpu_eff)}
 
     if rank == 0:
         line = {
@@ -485,10 +489,10 @@ def main():
             "dtype": "f32 (floatexp; f64 decisions)",
             "data": "synthetic",
             "config": {
-                "workload": "C2: two 1920x1080 frames (half-width 1e-300 and 1e-1000) at 1e-(k+5) from the period-14164 nucleus, maxiter 1e6, bailout 2^8",
+                "workload": "1080p deep frames: C2's two (half-width 1e-300 and 1e-1000 at 1e-(k+5) from the period-14164 nucleus) and a 1e-1000 frame holding a whole period-1331 minibrot; maxiter 1e6, bailout 2^8",
                 "frames_per_step": len(vlist),
                 "resolution": "%dx%d" % (W, H),
-                "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 16.6 MB written per frame; no flush",
+                "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 8.3 MB written per frame; no flush",
                 "frame_ms": {v["label"]: float(ms / args.steps) for v, ms in zip(vlist, frame_ms)},
                 "frames": frames,
                 "autotuned": tuning,
@@ -497,11 +501,15 @@ def main():
                 "reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_batch_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": eb_t / 2 * 1e3,
-                    "api": "mbx_compute_batch (both frames per call, host buffers, fresh GMP references)",
+                    "api": "mbx_compute_batch (all frames per call, host buffers, fresh GMP references)",
                     "per_frame_api": {"value": e2e_value, "frame_ms": e2e_t / len(vlist) * 1e3, "api": "mbx_compute, one frame per call"}},
             "plain_fp64": {"value": plain_value, "unit": UNIT, "sample": "%dx%d" % (pw, ph), "frame_ms_scaled_to_1080p": plain_frame_ms},
             "tuned_vs_plain": value / plain_value if plain_value > 0 else None,
-            "learned_1e-1000_vs_plain": (plain_frame_ms[[v["label"] for v in vlist].index("1e-1000")] / batched["learned_order"]["frame_1e-1000_ms"]) if "frame_1e-1000_ms" in batched.get("learned_order", {}) else None,
+            # per frame: plain FP64 frame time over the tuned form's (mixed, one
+            # frame per mbx_compute) and over the learned-scheduled batch form's
+            "vs_plain_per_frame": {v["label"]: {"mixed": plain_frame_ms[i] / frames[v["label"]]["frame_ms"],
+                                                 "mixed_learned": (plain_frame_ms[i] / batched["learned_order"]["frame_ms"][v["label"]]) if v["label"] in batched["learned_order"]["frame_ms"] else None}
+                                   for i, v in enumerate(vlist)},
             "accuracy": {"vs_truth": truth_acc,
                          "vs_exact_fp64": {"escape_iteration_identical": agree / total if total else None, "class_mismatch": cls_mis, "samples": total}},
             "roofline": {"bound": "fp32", "kernel": "k_lane_pass<float> (FP32 lane passes: probe + main)", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",

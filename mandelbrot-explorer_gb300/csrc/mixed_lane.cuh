@@ -462,6 +462,24 @@ MBX_HD void lane_refresh(Lane<T>& L) {
     L.di = ldexp_ftz(L.dcm.y * inv, L.dce - L.S.e);
 }
 
+// 2^k as a float, |k| <= 126.
+MBX_HD float pow2f(int k) { return bitsf((unsigned)(127 + k) << 23); }
+
+// Rescale of the FP32 lane by the power of two nearest |w|: with |w|^2 =
+// m 2^E (m in [1, 2)) and k = floor(E / 2), S.e += k, w and d scale by 2^-k,
+// s by 2^k and the error estimate (in units of S^2) by 2^-2k, all exactly, and
+// |w| lands in [1, 2 sqrt 2). Needs |w|^2 normal (the caller sends |w|^2 below
+// kWFloor on instead); k stays within [-50, 27] for the windows in use.
+MBX_HD void lane_rescale_pow2(Lane<float>& L, float wm2) {
+    const int k = ((int)((fbits(wm2) >> 23) & 0xffu) - 127) >> 1;
+    L.S.e += k;
+    const float sc = pow2f(-k);
+    L.wr *= sc;
+    L.wi *= sc;
+    L.err2 *= pow2f(-2 * k);
+    lane_refresh(L);
+}
+
 // dz = S w with S <- |v| 2^e and w <- v / |v| for a vector v scaled by 2^e.
 template <class T>
 MBX_HD void lane_set_delta(Lane<T>& L, T vr, T vi, int e) {
@@ -610,7 +628,9 @@ MBX_HD float lane_zc<float>(float x, float s, float w) { return fmaf(s, w, x); }
 // position, the wrap of a periodic orbit, maxiter or the end of the reference,
 // and the call's budget — so that a step carries no index tests; the first
 // iteration that could take a branch is left uncommitted for the general code,
-// which redoes it from the same state with the same operations. Per step: one
+// which redoes it from the same state with the same operations; a rescale
+// (|w|^2 out of its window) is done in place, exactly as the general code does
+// it (lane_rescale_pow2). Per step: one
 // 16-byte load of {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X +
 // 2 s w' as one paired FMA (so |2 z|^2 is the next error amplification g2 =
 // 4 |z|^2 exactly) and five compares. At a BLA position the per-position
@@ -624,18 +644,18 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
     int mlim = g.mxit - off; // m reaching mlim: maxiter, or the end of a non-periodic reference
     if (!per && reflen - 1 < mlim) mlim = reflen - 1;
     if (m0 + budget < mlim) mlim = m0 + budget;
-    const float s = L.s;
-    const float s2x5 = 5.0001f * (s * s); // |dz|^2 < |X|^2 / 5 as 5.0001 s^2 |w|^2 < |X|^2 (implies the general code's rebase screen)
+    float s = L.s;
+    float s2x5 = 5.0001f * (s * s); // |dz|^2 < |X|^2 / 5 as 5.0001 s^2 |w|^2 < |X|^2 (implies the general code's rebase screen)
     const float e4 = 4.0f * p.esc2lo;     // |2 z|^2 > 4 ESC2lo: the escape screen on 4 |z|^2 (exact scaling)
     const float wmax2 = p.wmax2, wmin2 = p.wmin2;
     const int blamask = (1 << minlevel) - 1;
     float wr = L.wr, wi = L.wi;
-    const float dr = L.dr, di = L.di;
+    float dr = L.dr, di = L.di;
     float err2 = L.err2, g2 = L.g2;
     float2 X2 = make_float2(L.Xc.x + L.Xc.x, L.Xc.y + L.Xc.y);
     int m = m0, rm = L.rm;
 #ifdef __CUDA_ARCH__
-    const float2 ss = make_float2(s, s), ss2 = make_float2(s + s, s + s);
+    float2 ss = make_float2(s, s), ss2 = make_float2(s + s, s + s);
 #endif
     for (;;) {
         if (m >= mlim) break;
@@ -683,13 +703,32 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
             const float ne = fmaf(err2, g2, R::kEps2 * wm2);
             // (|w| = 0 and the precision cap both leave through the |w|^2
             // tests; a NaN fails them too)
-            const bool common = !(g2n > e4) && ne <= kLaneCap2 * wm2 && wm2 <= wmax2 && wm2 >= wmin2 && s2x5 * wm2 < Xn.z;
+            const bool common = !(g2n > e4) && ne <= kLaneCap2 * wm2 && wm2 >= R::kWFloor && s2x5 * wm2 < Xn.z;
             if (!common) break;
             wr = nwr;
             wi = nwi;
             err2 = ne;
             g2 = g2n;
             X2 = make_float2(Xn.x, Xn.y);
+            if (!(wm2 <= wmax2 && wm2 >= wmin2)) {
+                // |w| left the window: the general code's rescale, in place
+                // (the rebase screen above is invariant under it)
+                L.wr = wr;
+                L.wi = wi;
+                L.err2 = err2;
+                lane_rescale_pow2(L, wm2);
+                wr = L.wr;
+                wi = L.wi;
+                err2 = L.err2;
+                s = L.s;
+                dr = L.dr;
+                di = L.di;
+                s2x5 = 5.0001f * (s * s);
+#ifdef __CUDA_ARCH__
+                ss = make_float2(s, s);
+                ss2 = make_float2(s + s, s + s);
+#endif
+            }
         }
         m += k;
         if (k > 0) rm = nidx + k - 1;
@@ -1015,13 +1054,17 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
             // |w| fell below the type's floor in one step (a near-zero |2 z|):
             // the absolute estimate err2 ~ |w|^2 may have left the normal range
             if (R::kTrackError && wm2 < Z(R::kWFloor)) return 3;
-            const T wmag = T(tsqrt(wm2)), inv = T(1) / wmag;
-            L.S = te_mulr(L.S, wmag);
-            L.wr *= inv;
-            L.wi *= inv;
-            // err2 in the new units: err2 inv^2 = err2 / |w|^2 (no overflow of inv^2)
-            if (R::kTrackError) L.err2 = L.err2 / (typename R::E)wm2;
-            lane_refresh(L);
+            if constexpr (std::is_same<T, float>::value) {
+                lane_rescale_pow2(L, wm2); // exact, as the common-step loop does it
+            } else {
+                const T wmag = T(tsqrt(wm2)), inv = T(1) / wmag;
+                L.S = te_mulr(L.S, wmag);
+                L.wr *= inv;
+                L.wi *= inv;
+                // err2 in the new units: err2 inv^2 = err2 / |w|^2 (no overflow of inv^2)
+                if (R::kTrackError) L.err2 = L.err2 / (typename R::E)wm2;
+                lane_refresh(L);
+            }
         }
         // Rebase (mp.cpp:3584-3615): |z|^2 < |dz|^2 decided on floatexp with a
         // 1e-4 margin; FP64 floatexp inside the margin, for strong

@@ -540,7 +540,8 @@ def create_compute_backend(requested: str = "cuda", device: int = 0) -> CudaComp
 def find_nucleus(center_re: str, center_im: str, radius: str, max_period: int, precision_bits: int):
     """Host-only nucleus search: returns (period, nucleus_re, nucleus_im, log10 size) or None."""
     lib = load_library()
-    n = precision_bits // 3 + 64
+    # digits of the precision plus room for the leading zeros of a small component
+    n = precision_bits // 3 + 64 + 8192
     a = ctypes.create_string_buffer(n)
     b = ctypes.create_string_buffer(n)
     sz = ctypes.c_double(0.0)
