@@ -158,7 +158,8 @@ def profile_run(args, vlist):
         out[v["label"]] = {"frame_ms": float(np.mean(times)), "pass_gpu_ms": st["pass_gpu_ms"], "fp32_pass_gpu_ms": st["fp32_pass_gpu_ms"], "rerun_gpu_ms": st["rerun_gpu_ms"],
                            "exact_form_gpu_ms": st["rerun_fp64_gpu_ms"], "fp64_reruns": st["fp64_reruns"], "exact_reruns": st["exact_reruns"], "steps": st["steps"],
                            "bla_applies": st["bla_applies"], "fp32_pass_steps": st["fp32_pass_steps"], "fp32_pass_bla_applies": st["fp32_pass_bla_applies"],
-                           "interior": st["interior"], "color_gpu_ms": be.last_color_stats()[0]}
+                           "interior": st["interior"], "fp32_unvouched_interior": st["fp32_unvouched_interior"], "fp32_unvouched_escape": st["fp32_unvouched_escape"],
+                           "color_gpu_ms": be.last_color_stats()[0]}
         be.close()
     print(json.dumps({"profile": out, "resolution": "%dx%d" % (args.width, args.height)}))
 

@@ -30,7 +30,7 @@ extern "C" {
 
 /* Arithmetic of the per-sample delta loop. */
 #define MBX_PRECISION_EXACT 0 /* FP64 / FP64-floatexp in the reference's exact operation order */
-#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration (floatexp frames without DE colouring; others take the exact form) */
+#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration with rebasing, for every perturbation frame (scale > 1e6) without DE colouring; others take the exact form */
 
 /* Status codes (the reference returns bool + ComputeBackendInfo strings). */
 #define MBX_OK 0
@@ -95,6 +95,8 @@ typedef struct {
     double fp32_pass_gpu_ms;        /* mixed form: CUDA-event time of the FP32 lane passes alone (probe and main) */
     long long fp32_pass_steps;      /* mixed form: delta steps executed by those passes */
     long long fp32_pass_bla_applies;/* mixed form: BLA skips taken by those passes */
+    long long fp32_unvouched_interior; /* mixed form: of fp64_reruns, interior decisions the FP32 estimate could not vouch for */
+    long long fp32_unvouched_escape;   /* mixed form: of fp64_reruns, escapes with |z|^2 within the estimated error of the bailout */
 } mbx_stats;
 
 /* createComputeBackend("cuda") (src/engine/compute_backend.cpp:277-290). Returns

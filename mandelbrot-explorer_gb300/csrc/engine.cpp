@@ -1488,6 +1488,8 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         if (cudaEventElapsedTime(&fms, ev0_, evm_) == cudaSuccess) stats_.fp32_pass_gpu_ms += fms;
         stats_.fp32_pass_steps += (long long)hctr_[0].steps;
         stats_.fp32_pass_bla_applies += (long long)hctr_[0].bla_applies;
+        stats_.fp32_unvouched_interior += (long long)hctr_[0].interior_flagged;
+        stats_.fp32_unvouched_escape += (long long)hctr_[0].escape_flagged;
     }
     if (cancel_.load()) return MBX_E_CANCELLED;
     if ((hctr_[0].stage_timeouts | hctr_[1].stage_timeouts) >> 16) {
@@ -2012,6 +2014,11 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     interior_eps2_ = 3e-9 * 3e-9;
     interior_confirm_ = 4;
     use_floatexp_ = mpf_cmp_d(scale, 1e280) > 0;
+    // The mixed form's lanes rebase (a delta whose |z| falls below |dz| restarts
+    // from the start of the reference), so one floatexp reference serves frames
+    // of any depth: its frames below the reference's floatexp gate (mp.cpp:
+    // 1573-1576) take the floatexp path too, with no glitch re-reference passes.
+    if (mixed_active()) use_floatexp_ = true;
     fe_cutoff_sensitive_ = false;
     dxfe_ = mpf_fe(dx_);
     dyfe_ = mpf_fe(dy_);

@@ -125,6 +125,7 @@ struct Counters {
     unsigned int finished;               // mixed pass: entries finished or queued
     unsigned int gmp_flags;              // floatexp pass: entries flagged for the arbitrary-precision recompute
     unsigned int interior_flagged;       // lane passes: interior decisions queued for the next tier
+    unsigned int escape_flagged;         // lane passes: escapes queued for the next tier (|z|^2 too near the bailout for the estimate)
     unsigned int probe_hit;              // interior gate probe: set by the first interior decision (the probe then stops)
     unsigned long long exact_steps;      // lane passes: steps taken in floatexp (orbit or delta below the lane's range)
     unsigned long long fe_rebases;       // lane passes: rebases decided in floatexp

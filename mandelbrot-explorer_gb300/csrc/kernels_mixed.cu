@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     const unsigned lane_id = threadIdx.x & 31;
     // per-thread counts of one pass (32-bit: a thread executes far fewer than
     // 2^32 steps per pass); skipped and effective iterations stay 64-bit
-    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0, n_intflag = 0;
+    unsigned n_steps = 0, n_bla = 0, n_rebase = 0, n_exact = 0, n_ferebase = 0, n_intflag = 0, n_escflag = 0;
     unsigned long long n_skip = 0, n_eff = 0;
     unsigned int n_int = 0, n_fin = 0;
     Lane<T> L;
@@ -205,6 +205,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
                 live = false;
             } else if (LaneReal<T>::kTrackError && st >= 3) { // queued for the next tier
                 if (st == 4) ++n_intflag;
+                if (st == 5) ++n_escflag;
                 int a[4];
                 entry_coords(f.px, L.i, a);
                 const unsigned q = atomicAdd(&f.ctr->rerun_n, 1u);
@@ -229,6 +230,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
     atomicAdd(&f.ctr->fe_rebases, (unsigned long long)n_ferebase);
     atomicAdd(&f.ctr->finished, n_fin);
     if (n_intflag) atomicAdd(&f.ctr->interior_flagged, n_intflag);
+    if (n_escflag) atomicAdd(&f.ctr->escape_flagged, n_escflag);
     atomicAdd(&f.ctr->interior, n_int);
     if (stage_late && !mbar_wait_bounded((unsigned)__cvta_generic_to_shared(&mbar), 1 << 24) && threadIdx.x == 0) atomicAdd(&f.ctr->stage_timeouts, 1u << 16);
 }

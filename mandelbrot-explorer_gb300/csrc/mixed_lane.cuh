@@ -755,8 +755,10 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 }
 
 // Advance one lane by up to `budget` iterations. Returns 0 running, 1 escaped,
-// 2 interior, 3 precision spent and 4 an unvouched interior decision (lanes
-// with an error estimate: rerun in the next tier); zrad_out is set on escape.
+// 2 interior, and for lanes with an error estimate (rerun in the next tier) 3
+// precision spent, 4 an unvouched interior decision, 5 an unvouched escape
+// (|z|^2 at N or N - 1 within the estimated error of the bailout); zrad_out is
+// set on escape.
 // INTR = false compiles the lane without its interior detectors, for passes
 // whose interior detection is off (exterior frames after the probe): their
 // state then takes no registers.
@@ -990,7 +992,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     const float sf = R::tof(L.s), wrf = R::tof(L.wr), wif = R::tof(L.wi), zf = (float)zesc, Ef = (float)ESC2z;
                     const float dzm2 = sf * sf * (wrf * wrf + wif * wif);
                     const float amb = 4.0f * sqrtf((float)lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
-                    if (!(zf >= Ef * (1.0f + amb)) || !(0.25f * L.g2 <= Ef * (1.0f - amb))) return 3; // (a NaN estimate fails too)
+                    if (!(zf >= Ef * (1.0f + amb)) || !(0.25f * L.g2 <= Ef * (1.0f - amb))) return 5; // (a NaN estimate fails too)
                 }
                 return 1;
             }

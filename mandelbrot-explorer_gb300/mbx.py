@@ -118,6 +118,8 @@ class Stats(ctypes.Structure):
         ("fp32_pass_gpu_ms", ctypes.c_double),
         ("fp32_pass_steps", ctypes.c_longlong),
         ("fp32_pass_bla_applies", ctypes.c_longlong),
+        ("fp32_unvouched_interior", ctypes.c_longlong),
+        ("fp32_unvouched_escape", ctypes.c_longlong),
     ]
 
     def as_dict(self):

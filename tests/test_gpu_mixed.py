@@ -42,8 +42,10 @@ def test_mixed_on_parity_cases(backend):
     reference's arbitrary-precision golden files are held to the tolerances its
     verify harness applies to its engine (TRUTH_TOL); the others to class
     agreement with the exact form and 99.9 % identical escape iterations. DE
-    colourings have no FP32 form and must come out identical to the exact form;
-    frames shallower than the floatexp range take the exact form too."""
+    colourings have no FP32 form and must come out identical to the exact form.
+    Frames shallower than the reference's floatexp gate (scale 1e6..1e280) run
+    the mixed form's rebasing floatexp lanes with one reference, where the exact
+    form runs the double path with glitch re-reference passes."""
     from conftest import GOLDEN
 
     cases = load_cases()

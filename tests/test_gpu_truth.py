@@ -55,3 +55,32 @@ def test_mixed_vs_truth_1080p(label):
     assert cls == 0
     assert same >= MIN_SAME
     assert dmu <= MAX_DMU
+
+
+def test_mixed_c1_config_vs_oracle():
+    """The plain FP64 configuration (views.c1_view: 1280x720, half-width 1e-30,
+    maxiter 50000) in the mixed form, below the reference's floatexp gate: the
+    rebasing FP32 lanes with one reference, against the oracle's exact double
+    path (mp.cpp:2290-2585): class identical everywhere and at least 99.99 % of
+    the escape iterations identical."""
+    import oracle
+
+    v = views.c1_view()
+    be = mbx.create_compute_backend("cuda")
+    try:
+        req = mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], 1280, 720, v["max_iterations"], bailout=v["bailout"], precision_mode=mbx.PRECISION_MIXED)
+        assert be.compute_status(req) == mbx.OK, be.last_error()
+        st = be.last_stats.as_dict()
+    finally:
+        be.close()
+    assert st["used_floatexp"] == 1
+    oit, _, oen, _ = oracle.render(v["center_re"], v["center_im"], v["scale"], 1280, 720, v["max_iterations"], bailout=v["bailout"])
+    en = req.escape_iteration
+    same = float(np.mean(en == oen))
+    cls = int(np.sum((en < 0) != (oen < 0)))
+    ext = (en > 0) & (oen > 0)
+    dmu = float(np.max(np.abs(req.iterations[ext].astype(np.float64) - oit[ext]), initial=0.0))
+    print("\n[c1 mixed] N identical to the exact double path %.6f, class mismatches %d, max |dmu| %.4g, double-float reruns %d" % (same, cls, dmu, st["fp64_reruns"]))
+    assert cls == 0
+    assert same >= MIN_SAME
+    assert dmu <= MAX_DMU
