@@ -201,8 +201,8 @@ int BatchRunner::schedule_gradient(const float* features, const float* targets, 
     return e == cudaSuccess ? MBX_OK : cuda_fail(err, "gradient check", e);
 }
 
-int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, std::string& err) {
-    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag && g_schedule_ == schedule_) return MBX_OK;
+int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, int deriv, std::string& err) {
+    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag && g_schedule_ == schedule_ && g_deriv_ == deriv) return MBX_OK;
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     exec_ = nullptr;
@@ -222,6 +222,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.capacity = cap_samples_;
         a.view_interior = vint;
         a.cancel = cancel_flag;
+        a.deriv = deriv;
         // FP32 over all samples (in the learned order when given)
         a.total = total;
         a.queue = order;
@@ -258,6 +259,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     g_main_ = main_total;
     g_cancel_ = cancel_flag;
     g_schedule_ = schedule_;
+    g_deriv_ = deriv;
     return MBX_OK;
 }
 
@@ -332,7 +334,9 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
         cudaMemcpyAsync(d_probe_, h_desc_, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
         cudaMemcpyAsync(d_main_, h_desc_ + nv, sizeof(ViewDesc) * nv, cudaMemcpyHostToDevice, st_);
         bs.h2d_bytes += (long long)(sizeof(unsigned) + 2 * sizeof(ViewDesc) * nv);
-        rc = build_graph(nv, probe_total, main_total, cancel_flag, err);
+        int deriv = 0;
+        for (int k = 0; k < nv; ++k) deriv |= h_desc_[nv + k].p.g.deriv ? 1 : 0;
+        rc = build_graph(nv, probe_total, main_total, cancel_flag, deriv, err);
         if (rc != MBX_OK) return rc;
         cudaEventRecord(ev0_, st_);
         cudaError_t e = cudaGraphLaunch(exec_, st_);

@@ -31,7 +31,7 @@ class BatchRunner {
   private:
     int ensure_engines(int n, std::string& err);
     int ensure_buffers(int nviews, unsigned capacity, std::string& err);
-    int build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, std::string& err);
+    int build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, int deriv, std::string& err);
 
     int device_;
     std::vector<std::unique_ptr<Engine>> eng_;
@@ -53,6 +53,7 @@ class BatchRunner {
     unsigned g_probe_ = 0, g_main_ = 0;
     volatile int* g_cancel_ = nullptr;
     int g_schedule_ = -1;
+    int g_deriv_ = -1;     // the captured graph's lanes carry the derivative (DE colourings)
     // learned ordering
     int schedule_ = 0;
     SchedState sched_{};

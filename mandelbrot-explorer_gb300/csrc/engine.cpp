@@ -1803,6 +1803,7 @@ void Engine::fill_batch_slot() {
     pr.f.px.skip_i = pr.f.px.skip_j = -1;
     pr.f.px.n = ((H_ + 7) / 8) * ((W_ + 7) / 8);
     pr.p.use_interior = 1;
+    pr.p.g.ede = pr.p.g.deovl = pr.p.g.normal = pr.p.g.deriv = 0; // the probe needs no DE values
     pr.count = (unsigned)pr.f.px.n;
     // main pass over the frame minus the reference pixel
     ViewDesc mn = d;

@@ -281,6 +281,7 @@ struct BatchArgs {
     unsigned* view_interior; // probe pass: interior count per view (null otherwise)
     volatile int* cancel;
     unsigned wide_from = 0;  // as MixedParams::wide_from
+    int deriv = 0;           // some view has a DE colouring: the lanes that carry the derivative
 };
 // Rerun queues at least this many entries per SM take 32 lanes per warp
 // (fewer warp instructions for the same samples); shorter ones 8 (less

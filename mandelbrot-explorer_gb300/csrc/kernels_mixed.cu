@@ -56,6 +56,38 @@ __device__ __forceinline__ float tlog2(float x) { return log2f(x); }
 __device__ __forceinline__ double tlog2(double x) { return log2(x); }
 __device__ __forceinline__ float tlog2(df32 x) { return log2f(x.hi + x.lo); }
 
+// Results of a lane (pixelRescaled's outputs, mp.cpp:3498-3528): the smooth
+// value N - log2(log2|z|) in the lane type; under DE colourings the distance
+// |z| log|z|^2 / (dx |J|) in FP64 floatexp (into the values under EDE, into the
+// normal buffer under the DE overlay) or the normal-map angle arg z - arg J;
+// EDE takes precedence, then the normal map. The normal buffer holds 0 where
+// the exact form writes no angle or distance.
+template <bool DE, class T>
+__device__ __forceinline__ void lane_write_escape(const Outputs& o, const FrameGeom& g, const MixedParams& p, const Lane<T>& L, T zrad) {
+    float v = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
+    if (DE && g.deriv) {
+        float nrm = 0.0f;
+        if (g.ede || (g.deovl && !g.normal)) {
+            const double zr2 = (double)zrad;
+            const double num = sqrt(zr2) * log(zr2);
+            const float de = (float)fe_to_double(fe_div(fe_from(num), fe_mul(p.dxfe, lane_j_mag(L))));
+            if (g.ede) v = de;
+            else nrm = de;
+        } else if (g.normal) {
+            nrm = (float)(atan2((double)L.ezi, (double)L.ezr) - atan2((double)L.ji, (double)L.jr));
+        }
+        if ((g.deovl || g.normal) && o.normal) o.normal[L.oidx] = nrm;
+    }
+    o.iter[L.oidx] = v;
+    if (o.escN) o.escN[L.oidx] = L.iter;
+}
+template <bool DE, class T>
+__device__ __forceinline__ void lane_write_interior(const Outputs& o, const FrameGeom& g, const Lane<T>& L) {
+    o.iter[L.oidx] = -2.0f;
+    if (DE && g.deriv && (g.deovl || g.normal) && o.normal) o.normal[L.oidx] = 0.0f;
+    if (o.escN) o.escN[L.oidx] = -1;
+}
+
 // Bounded wait on phase 0 of an mbarrier: true once the phase completed, false
 // after `limit` polls.
 __device__ bool mbar_wait_bounded(unsigned mb, int limit) {
@@ -105,7 +137,7 @@ constexpr int kLaneBudget = 256;
 // LANES < 32: only the low LANES lanes of a warp take samples. The rerun
 // passes are latency-bound (few samples, long dependency chains), so spreading
 // their samples over more warps hides more latency than filling each warp.
-template <class T, int MAXT, int MINB, int LANES = 32, bool INTR = true, bool FASTI = false>
+template <class T, int MAXT, int MINB, int LANES = 32, bool INTR = true, bool FASTI = false, bool DE = false>
 __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedParams p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orbit) {
     using V2 = typename LaneReal<T>::V2;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -137,7 +169,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         }
     }
     const int reflen = p.mx_ref_it + 1;
-    const T ESC2f = (T)g.ESC2;
+    const T ESC2f = T(p.esc2f); // (unused by the lanes; no FP64 conversion)
     const int blamask = (1 << f.bla.minlevel) - 1;
     const BlaEntry<T>* bt = f.bla.use ? blat : nullptr;
     const TE<T> dxf = te_from_fe<T>(p.dxfe), dyf = te_from_fe<T>(p.dyfe);
@@ -184,20 +216,17 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         }
         if (live) {
             T zrad = T(0);
-            const int st = lane_run<T, INTR, FASTI>(L, kLaneBudget, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
+            const int st = lane_run<T, INTR, FASTI, DE>(L, kLaneBudget, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (p.probe_stop && (st == 2 || st == 4)) atomicExch(&f.ctr->probe_hit, 1u);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
-                // smooth value N - log2(log2|z|) in the lane type (the output is FP32)
-                f.out.iter[L.oidx] = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
-                if (f.out.escN) f.out.escN[L.oidx] = L.iter;
+                lane_write_escape<DE>(f.out, g, p, L, zrad);
                 f.out.done[L.i] = 1;
                 ++n_fin;
                 n_eff += (unsigned long long)L.iter;
                 live = false;
             } else if (st == 2) {
-                f.out.iter[L.oidx] = -2.0f;
-                if (f.out.escN) f.out.escN[L.oidx] = -1;
+                lane_write_interior<DE>(f.out, g, L);
                 f.out.done[L.i] = 1;
                 ++n_fin;
                 n_eff += (unsigned long long)g.mxit;
@@ -254,7 +283,7 @@ struct ViewTables<df32> {
 // finish one view's samples continue with another's), the rerun passes take a
 // queue whose keys carry the view index. Each lane reads its view's descriptor
 // from device memory; lanes of one warp may work on different views.
-template <class T, int MAXT, int MINB, int LANES = 32>
+template <class T, int MAXT, int MINB, int LANES = 32, bool DE = false>
 __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
     using V2 = typename LaneReal<T>::V2;
     __shared__ unsigned s_base[kBatchMaxViews];
@@ -326,18 +355,16 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
             const ViewDesc& vd = a.views[view];
             const BlaEntry<T>* bt = vd.f.bla.use ? ViewTables<T>::bla(vd) : nullptr;
             T zrad = T(0);
-            const int st = lane_run(L, kLaneBudget, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, (T)vd.p.g.ESC2, (1 << vd.f.bla.minlevel) - 1, zrad,
-                                    n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
+            const int st = lane_run<T, true, false, DE>(L, kLaneBudget, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, T(vd.p.esc2f), (1 << vd.f.bla.minlevel) - 1, zrad,
+                                                       n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (st != 0 && vd.f.out.cost) vd.f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
-                vd.f.out.iter[L.oidx] = (float)((T)L.iter - tlog2(T(0.5) * tlog2(zrad)));
-                if (vd.f.out.escN) vd.f.out.escN[L.oidx] = L.iter;
+                lane_write_escape<DE>(vd.f.out, vd.p.g, vd.p, L, zrad);
                 ++n_fin;
                 n_eff += (unsigned long long)L.iter;
                 live = false;
             } else if (st == 2) {
-                vd.f.out.iter[L.oidx] = -2.0f;
-                if (vd.f.out.escN) vd.f.out.escN[L.oidx] = -1;
+                lane_write_interior<DE>(vd.f.out, vd.p.g, L);
                 if (a.view_interior) atomicAdd(&a.view_interior[view], 1u);
                 ++n_fin;
                 n_eff += (unsigned long long)vd.p.g.mxit;
@@ -531,8 +558,10 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
     DeviceFrame g = f;
     if (!(bla_.use && dbla32_.p)) g.bla.use = 0;
     // the interior gate's probe stops at its first interior decision (unless
-    // its per-sample costs are wanted)
+    // its per-sample costs are wanted); it needs no DE values (the main pass
+    // renders its samples again)
     p.probe_stop = (probe_gate_only_ && !g.out.cost) ? 1 : 0;
+    if (probe_gate_only_) p.g.ede = p.g.deovl = p.g.normal = p.g.deriv = 0;
     auto launch = [&](auto kern) -> cudaError_t {
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -543,6 +572,10 @@ cudaError_t Engine::run_mixed_pass(const DeviceFrame& f) {
     };
     if (probe_gate_only_ && threads == 256 && mixed_blocks_per_sm_ == 3) // the probe: common iterations in the fast loop too
         return launch(k_lane_pass<float, 256, 3, 32, true, true>);
+    if (p.g.deriv) { // DE colourings: the lanes carry the derivative (one launch shape)
+        if (!p.use_interior) return launch(k_lane_pass<float, 256, 3, 32, false, false, true>);
+        return launch(k_lane_pass<float, 256, 3, 32, true, false, true>);
+    }
     if (!p.use_interior) { // exterior after the probe: the lane without interior detectors
         if (mixed_blocks_per_sm_ >= 4) return launch(k_lane_pass<float, 256, 4, 32, false>);
         if (mixed_blocks_per_sm_ == 3) return launch(k_lane_pass<float, 256, 3, 32, false>);
@@ -567,8 +600,8 @@ cudaError_t Engine::run_df_pass(const DeviceFrame& f) {
     // the queue length is known only on the device: both widths are launched
     // and the one it selects runs
     p.wide_from = kWideLanesPerSm * (unsigned)nsm_;
-    auto narrow = k_lane_pass<df32, 128, 2, 8>;
-    auto wide = k_lane_pass<df32, 128, 2, 32>;
+    auto narrow = p.g.deriv ? k_lane_pass<df32, 128, 2, 8, true, false, true> : k_lane_pass<df32, 128, 2, 8>;
+    auto wide = p.g.deriv ? k_lane_pass<df32, 128, 2, 32, true, false, true> : k_lane_pass<df32, 128, 2, 32>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(narrow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -583,12 +616,18 @@ cudaError_t Engine::run_df_pass(const DeviceFrame& f) {
 // (what it cannot vouch for goes to each view's exact form on the host side).
 cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st) {
     if (tier == 0) {
-        k_batch_pass<float, 256, 3><<<nsm * 3, 256, 0, st>>>(a);
+        if (a.deriv) k_batch_pass<float, 256, 3, 32, true><<<nsm * 3, 256, 0, st>>>(a);
+        else k_batch_pass<float, 256, 3><<<nsm * 3, 256, 0, st>>>(a);
     } else {
         BatchArgs b = a;
         b.wide_from = kWideLanesPerSm * (unsigned)nsm;
-        k_batch_pass<df32, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(b);
-        k_batch_pass<df32, 128, 2, 32><<<nsm * 4, 128, 0, st>>>(b);
+        if (a.deriv) {
+            k_batch_pass<df32, 128, 2, 8, true><<<nsm * 4, 128, 0, st>>>(b);
+            k_batch_pass<df32, 128, 2, 32, true><<<nsm * 4, 128, 0, st>>>(b);
+        } else {
+            k_batch_pass<df32, 128, 2, 8><<<nsm * 4, 128, 0, st>>>(b);
+            k_batch_pass<df32, 128, 2, 32><<<nsm * 4, 128, 0, st>>>(b);
+        }
     }
     return cudaGetLastError();
 }

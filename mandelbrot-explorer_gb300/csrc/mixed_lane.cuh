@@ -347,7 +347,7 @@ MBX_HDF BlaEntry<T> bla_entry(double v, double4 c) {
 // w into the new units.
 template <class T>
 MBX_HDF int lane_bla(const BlaView& b, const BlaEntry<T>* t, const typename LaneReal<T>::V2* orb, bool periodic, int s, TE<T>& S, T& wr, T& wi,
-                     typename LaneReal<T>::V2 dcm, int dce, typename LaneReal<T>::Z ESC2lo, int mx_ref_it, float& amp2) {
+                     typename LaneReal<T>::V2 dcm, int dce, typename LaneReal<T>::Z ESC2lo, int mx_ref_it, float& amp2, BlaEntry<T>* used = nullptr) {
     using R = LaneReal<T>;
     using Z = typename R::Z;
     int maxp = b.nlev - 1;
@@ -394,6 +394,7 @@ MBX_HDF int lane_bla(const BlaView& b, const BlaEntry<T>* t, const typename Lane
             wr = vr * inv;
             wi = vi * inv;
         }
+        if (used) *used = e;
         return l;
     }
     return 0;
@@ -452,6 +453,10 @@ struct Lane {
     double zsr, zsi, conf_zr, conf_zi;
     TE<T> sS;
     int save_iter, period_win, conf_P, conf_next, conf_count, conf_giveup, sidx, save_iter2, twin2;
+    // derivative J = dz/dc of the DE colourings: J = SJ (jr, ji) with invSJ =
+    // 1 / SJ in the lane type (0 below its range); ezr, ezi: z at the escape
+    TE<T> SJ;
+    T jr, ji, invSJ, ezr, ezi;
 };
 
 template <class T>
@@ -478,6 +483,120 @@ MBX_HD void lane_rescale_pow2(Lane<float>& L, float wm2) {
     L.wi *= sc;
     L.err2 *= pow2f(-2 * k);
     lane_refresh(L);
+}
+
+// ---- the derivative J = dz/dc (DE colourings) ------------------------------
+// As in the reference's rescaled loop (mp.cpp:3348-3360, 3478-3511), J is
+// carried like the delta: a floatexp scale SJ and a unit-scale vector (jr, ji)
+// in the lane type, advancing as J' = 2 z J + 1 per step (z the pre-step
+// value; the "+1" is invSJ in the units of SJ) and as J' = A J + B through a
+// BLA skip. A rebase leaves J alone: it is the derivative of the reconstructed
+// z. The DE value is formed once per sample, in FP64 floatexp.
+MBX_HD double pow2d(int k) { return bitsd((uint64_t)(1023 + k) << 52); }
+template <class T>
+MBX_HD T lane_mul2k(T x, int k); // x 2^k, |k| <= 250 (exact unless the result leaves the normal range)
+template <>
+MBX_HD float lane_mul2k<float>(float x, int k) {
+    const int h = k / 2;
+    return (x * pow2f(h)) * pow2f(k - h);
+}
+template <>
+MBX_HD double lane_mul2k<double>(double x, int k) { return x * pow2d(k); }
+template <>
+MBX_HD df32 lane_mul2k<df32>(df32 x, int k) { return df32(lane_mul2k<float>(x.hi, k), lane_mul2k<float>(x.lo, k)); }
+
+template <class T>
+MBX_HD void lane_j_inv(Lane<T>& L) { L.invSJ = ldexp_ftz(T(1) / L.SJ.m, -L.SJ.e); }
+
+template <class T>
+MBX_HD void lane_j_init(Lane<T>& L) { // J_1 = d(dc)/dc = 1
+    L.SJ = TE<T>{T(0.5), 1};
+    L.jr = T(1);
+    L.ji = T(0);
+    L.invSJ = T(1);
+}
+
+// |j| back to [0.5, 1.5) when |j|^2 leaves [1e-16, 1e16]: SJ.e += k and j scaled
+// by 2^-k, with 2^k the binade of the larger component (exact).
+template <class T>
+MBX_HD void lane_j_window(Lane<T>& L) {
+    using R = LaneReal<T>;
+    using Z = typename R::Z;
+    const Z jm2 = R::zabs2(L.jr, L.ji);
+    if (jm2 <= Z(1e16) && jm2 >= Z(1e-16)) return;
+    const Z ar = tabs(R::z(L.jr)), ai = tabs(R::z(L.ji));
+    const Z amax = ar > ai ? ar : ai;
+    if (!(amax > Z(0))) { // the derivative vanished (or is not a number)
+        L.SJ = TE<T>{T(0.5), 1};
+        L.jr = L.ji = T(0);
+        lane_j_inv(L);
+        return;
+    }
+    const int k = te_norm(amax, 0).e; // amax = m 2^k, m in [0.5, 1)
+    L.SJ.e += k;
+    L.jr = lane_mul2k(L.jr, -k);
+    L.ji = lane_mul2k(L.ji, -k);
+    lane_j_inv(L);
+}
+
+// J' = 2 z J + 1 with z at unit scale in the lane type.
+template <class T>
+MBX_HD void lane_j_step(Lane<T>& L, T zr, T zi) {
+    const T a = T(2) * (zr * L.jr - zi * L.ji) + L.invSJ;
+    const T b = T(2) * (zr * L.ji + zi * L.jr);
+    L.jr = a;
+    L.ji = b;
+    lane_j_window(L);
+}
+// The FP32 lane's form, from 2 z = 2 X + 2 s w as the common-step loop forms it.
+MBX_HD void lane_j_step_2z(Lane<float>& L, float z2r, float z2i) {
+    const float a = fmaf(z2r, L.jr, fmaf(-z2i, L.ji, L.invSJ));
+    const float b = fmaf(z2r, L.ji, z2i * L.jr);
+    L.jr = a;
+    L.ji = b;
+    lane_j_window(L);
+}
+
+// J = (nr, ni) given in floatexp.
+template <class T>
+MBX_HDF void lane_j_set_fe(Lane<T>& L, FE nr, FE ni) {
+    const FE mag = fe_sqrt(fe_add(fe_mul(nr, nr), fe_mul(ni, ni)));
+    if (mag.m == 0.0) {
+        L.SJ = TE<T>{T(0.5), 1};
+        L.jr = L.ji = T(0);
+    } else {
+        L.SJ = te_from_fe<T>(mag);
+        L.jr = (T)fe_to_double(fe_div(nr, mag));
+        L.ji = (T)fe_to_double(fe_div(ni, mag));
+    }
+    lane_j_inv(L);
+}
+// J' = 2 z J + 1 with z in floatexp: the steps where z lies outside the lane
+// type's range (the exact floatexp steps; rare).
+template <class T>
+MBX_HDF void lane_j_step_fe(Lane<T>& L, FE zr, FE zi) {
+    const FE sj = fe_from_te(L.SJ);
+    const FE Jr = fe_mul_d(sj, (double)L.jr), Ji = fe_mul_d(sj, (double)L.ji);
+    const FE nr = fe_add(fe_scale2(fe_sub(fe_mul(zr, Jr), fe_mul(zi, Ji)), 1), fe_make(0.5, 1));
+    const FE ni = fe_scale2(fe_add(fe_mul(zr, Ji), fe_mul(zi, Jr)), 1);
+    lane_j_set_fe(L, nr, ni);
+}
+// J' = A J + B through a BLA skip, with the entry's floatexp coefficients.
+template <class T>
+MBX_HDF void lane_j_bla(Lane<T>& L, const BlaEntry<T>& e) {
+    const FE sj = fe_from_te(L.SJ);
+    const FE Jr = fe_mul_d(sj, (double)L.jr), Ji = fe_mul_d(sj, (double)L.ji);
+    const FE Ar = fe_renorm((double)e.ar, e.ea), Ai = fe_renorm((double)e.ai, e.ea);
+    const FE Br = fe_renorm((double)e.br, e.eb), Bi = fe_renorm((double)e.bi, e.eb);
+    const FE nr = fe_add(fe_sub(fe_mul(Ar, Jr), fe_mul(Ai, Ji)), Br);
+    const FE ni = fe_add(fe_add(fe_mul(Ar, Ji), fe_mul(Ai, Jr)), Bi);
+    lane_j_set_fe(L, nr, ni);
+}
+// |J| in floatexp.
+template <class T>
+MBX_HDF FE lane_j_mag(const Lane<T>& L) {
+    const double jr = (double)L.jr, ji = (double)L.ji;
+    return fe_mul_d(fe_from_te(L.SJ), xsqrt(jr * jr + ji * ji));
 }
 
 // dz = S w with S <- |v| 2^e and w <- v / |v| for a vector v scaled by 2^e.
@@ -552,6 +671,7 @@ MBX_HDF void lane_setup_at(Lane<T>& L, int i, const int* arr, const MixedParams&
     L.twin2 = 1;
     L.err2 = LaneReal<T>::kEps2;
     L.g2 = 4.0f * lane_abs2f(L.Xc);
+    lane_j_init(L);
 }
 
 template <class T>
@@ -620,6 +740,17 @@ MBX_HD T lane_zc(T x, T s, T w) { return x + s * w; }
 template <>
 MBX_HD float lane_zc<float>(float x, float s, float w) { return fmaf(s, w, x); }
 
+// J' = 2 z J + 1 with z = X + s w of the lane's current (pre-step) state, in
+// the form both of the FP32 lane's paths use.
+template <class T>
+MBX_HD void lane_j_advance(Lane<T>& L) {
+    if constexpr (std::is_same<T, float>::value)
+        lane_j_step_2z(L, fmaf(L.s + L.s, L.wr, L.Xc.x + L.Xc.x), fmaf(L.s + L.s, L.wi, L.Xc.y + L.Xc.y));
+    else
+        lane_j_step(L, lane_zc<T>(L.Xc.x, L.s, L.wr), lane_zc<T>(L.Xc.y, L.s, L.wi));
+}
+
+
 // Common iterations of the FP32 lane without interior detection: iterations
 // that take none of the general code's branches (no BLA skip, orbit entry in
 // range, no escape screen, precision cap, rescale, rebase candidate or end of
@@ -636,6 +767,7 @@ MBX_HD float lane_zc<float>(float x, float s, float w) { return fmaf(s, w, x); }
 // 4 |z|^2 exactly) and five compares. At a BLA position the per-position
 // radius maximum decides: |dz|^2 not below it fails every level, so the
 // iteration is a common one. Returns the steps taken.
+template <bool DERIV>
 MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const MixedParams& p, int reflen, bool bla_on, int minlevel, const BlaMaxR2* bmax) {
     using R = LaneReal<float>;
     const float4* q = p.Zq;
@@ -657,6 +789,12 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
 #ifdef __CUDA_ARCH__
     float2 ss = make_float2(s, s), ss2 = make_float2(s + s, s + s);
 #endif
+    // DE: 2 z before the step, for J' = 2 z J + 1 (the general code's form)
+    float z2pr = 0.0f, z2pi = 0.0f;
+    if (DERIV) {
+        z2pr = fmaf(s + s, wr, X2.x);
+        z2pi = fmaf(s + s, wi, X2.y);
+    }
     for (;;) {
         if (m >= mlim) break;
         // the current orbit entry below the lane's range (also X = 0 after a rebase)
@@ -710,6 +848,11 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
             err2 = ne;
             g2 = g2n;
             X2 = make_float2(Xn.x, Xn.y);
+            if (DERIV) {
+                lane_j_step_2z(L, z2pr, z2pi);
+                z2pr = z2.x; // (a rescale below leaves 2 s w unchanged)
+                z2pi = z2.y;
+            }
             if (!(wm2 <= wmax2 && wm2 >= wmin2)) {
                 // |w| left the window: the general code's rescale, in place
                 // (the rebase screen above is invariant under it)
@@ -762,7 +905,7 @@ MBX_HD int lane_interior(const Lane<T>& L) {
 // INTR = false compiles the lane without its interior detectors, for passes
 // whose interior detection is off (exterior frames after the probe): their
 // state then takes no registers.
-template <class T, bool INTR = true, bool FASTI = false>
+template <class T, bool INTR = true, bool FASTI = false, bool DE = false>
 MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedParams& p, const BlaEntry<T>* blat, const typename LaneReal<T>::V2* orb,
                      int reflen, T ESC2f, int blamask, T& zrad_out, unsigned& n_steps, unsigned& n_bla, unsigned long long& n_skip,
                      unsigned& n_rebase, unsigned& n_exact, unsigned& n_ferebase) {
@@ -776,10 +919,13 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     // (float)ESC2 rounded on the host for the float-screen lanes: no FP64 conversion per call
     const Z ESC2z = std::is_same<Z, float>::value ? (Z)p.esc2f : (Z)g.ESC2;
     const Z ESC2hi = ESC2z * R::kEscHi, ESC2lo = ESC2z * R::kEscLo;
+    // DE colourings: the derivative J advances with the delta (DE lanes only)
+    const bool deriv = DE && g.deriv;
     for (int b = 0; b < budget; ++b) {
         if constexpr (std::is_same<T, float>::value && !FASTI) {
             if (!(INTR && p.use_interior) && p.Zq) {
-                const int took = lane_fast_f32(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax);
+                const int took = deriv ? lane_fast_f32<true>(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax)
+                                       : lane_fast_f32<false>(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax);
                 n_steps += (unsigned)took;
                 b += took;
                 if (b >= budget) return 0;
@@ -854,6 +1000,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     // |w|^2 tests: the general code handles them)
                     const bool rare = zrad > ESC2lo || !(nerr2 <= kLaneCap2 * (E)wm2) || wm2 > wmax2 || wm2 < wmin2 || !far;
                     if (rare) break;
+                    if (deriv) lane_j_advance(L); // (from the pre-step state)
                     L.wr = nwr;
                     L.wi = nwi;
                     L.err2 = nerr2;
@@ -885,8 +1032,10 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         }
         if (blat && L.m >= 2 && ((L.rm - 1) & blamask) == 0) {
             float amp2 = 0.0f;
-            const int skip = lane_bla(f.bla, blat, orb, per > 0, L.rm, L.S, L.wr, L.wi, L.dcm, L.dce, ESC2lo, per ? per : reflen, amp2);
+            BlaEntry<T> used;
+            const int skip = lane_bla(f.bla, blat, orb, per > 0, L.rm, L.S, L.wr, L.wi, L.dcm, L.dce, ESC2lo, per ? per : reflen, amp2, deriv ? &used : nullptr);
             if (skip > 0) {
+                if (deriv) lane_j_bla(L, used);
                 ++n_bla;
                 n_skip += skip;
                 L.m += skip;
@@ -917,6 +1066,15 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         // size) at a nucleus pass).
         const bool tiny = (L.m == 0 && !(L.s >= R::kMinS)) ||
                           (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0));
+        if (deriv) { // J' = 2 z J + 1 with the pre-step z (mp.cpp:3436-3441, 3478-3497)
+            if (!tiny) {
+                lane_j_advance(L);
+            } else { // z outside the lane type's range: in floatexp
+                const FE zero = fe_make(0.0, 0);
+                const FE S0 = fe_from_te(L.S);
+                lane_j_step_fe(L, fe_add(L.m ? Zfe[L.rm].re : zero, fe_mul_d(S0, (double)L.wr)), fe_add(L.m ? Zfe[L.rm].im : zero, fe_mul_d(S0, (double)L.wi)));
+            }
+        }
         if (!tiny) {
             T nwr, nwi;
             typename R::E nerr2;
@@ -994,6 +1152,8 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     const float amb = 4.0f * sqrtf((float)lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
                     if (!(zf >= Ef * (1.0f + amb)) || !(0.25f * L.g2 <= Ef * (1.0f - amb))) return 5; // (a NaN estimate fails too)
                 }
+                L.ezr = zr;
+                L.ezi = zi;
                 return 1;
             }
         }

@@ -10,6 +10,8 @@ figures; recomputing them takes minutes of GMP work per frame, so they travel
 with the repository.
 
 Usage: python tests/golden/make_truth.py [frame ...]   (default: every frame)
+       python tests/golden/make_truth.py --cases [case ...]  (full-frame truth of
+       double-path parity cases, truthgen_<case>.npz; default: CASE_TRUTH)
 """
 import os
 import sys
@@ -58,6 +60,35 @@ def make(label):
     print("%s: %d samples in %.0f s, %d interior, N %d..%d" % (label, SUBSET, time.time() - t, int(np.sum(tn < 0)), int(tn[tn > 0].min(initial=0)), int(tn.max())))
 
 
+# Double-path parity cases (tests/golden/cases.json, scale 1e6..1e280) that have
+# no arbitrary-precision golden file from the reference: full-frame truth, so
+# that forms which differ from the reference's double path on chaotic samples
+# can be compared with it on the same footing (tests/test_gpu_mixed.py).
+CASE_TRUTH = ("c1", "flake", "ticktock", "deep51")
+
+
+def case_path(name):
+    return os.path.join(HERE, "truthgen_%s.npz" % name)
+
+
+def make_case(name):
+    import json
+
+    c = json.load(open(os.path.join(HERE, "cases.json")))[name]
+    W, H = c["width"], c["height"]
+    rows, cols = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    keys = np.stack([rows.ravel(), cols.ravel(), np.zeros(W * H, int), np.zeros(W * H, int)], axis=1)
+    t = time.time()
+    tv, tn = oracle.truth(c["center_re"], c["center_im"], c["scale"], W, H, c["max_iterations"], keys, sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"], threads=os.cpu_count())
+    np.savez_compressed(case_path(name), N=tn.astype(np.int32), value=tv.astype(np.float32))
+    print("%s: %d samples in %.0f s, %d interior" % (name, W * H, time.time() - t, int(np.sum(tn < 0))))
+
+
 if __name__ == "__main__":
-    for label in sys.argv[1:] or views.TRUTH_FRAMES:
-        make(label)
+    args = sys.argv[1:]
+    if args and args[0] == "--cases":
+        for name in args[1:] or CASE_TRUTH:
+            make_case(name)
+    else:
+        for label in args or views.TRUTH_FRAMES:
+            make(label)
