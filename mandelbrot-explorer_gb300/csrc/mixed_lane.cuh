@@ -417,6 +417,10 @@ MBX_HDF int lane_bla(const BlaView& b, const BlaEntry<T>* t, const typename Lane
 // kept in float for every lane type.
 constexpr float kLaneInteriorTol2 = 1e-4f; // (1e-2)^2
 constexpr float kLaneCap2 = 0.25f;         // (1/2)^2
+// DE colourings: the derivative J follows the orbit, so its relative error is
+// of the order of the delta's; an escape's distance (or normal angle) is kept
+// only when the estimated relative error of dz is below 1e-4.
+constexpr float kLaneDeTol2 = 1e-8f;
 
 // Squared relative error estimate of the delta.
 template <class T>
@@ -1151,6 +1155,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                     const float dzm2 = sf * sf * (wrf * wrf + wif * wif);
                     const float amb = 4.0f * sqrtf((float)lane_rel_err2(L.err2, L.wr, L.wi) * dzm2 / zf);
                     if (!(zf >= Ef * (1.0f + amb)) || !(0.25f * L.g2 <= Ef * (1.0f - amb))) return 5; // (a NaN estimate fails too)
+                    if (deriv && !((float)lane_rel_err2(L.err2, L.wr, L.wi) <= kLaneDeTol2)) return 5;
                 }
                 L.ezr = zr;
                 L.ezi = zi;

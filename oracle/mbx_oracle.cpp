@@ -522,6 +522,12 @@ float Engine::shallowSimd(double cr, double ci, int mxit, int cm, int* nout) con
     }
 }
 
+// Truth of the normal-map angle (private flag of Engine::truth only): the same
+// GMP orbit and derivative dz/dc as the EDE branch, returning arg z_N - arg dz/dc
+// at the escape. The reference's point routine has no normal-map branch; its
+// render path (accuratePixel) never sets this flag.
+constexpr int kTruthAngle = 1 << 20;
+
 // mp.cpp:719-894 (smooth / EDE branches; derivative tracked, no env overrides).
 float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, int* nout) const {
     if (nout) *nout = -1;
@@ -533,6 +539,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
     mpf_init2(d_re, wp); mpf_init2(d_im, wp);
     mpf_set_str(d_re, "2", 10);
     const bool ede = (cm & CM_EDE) != 0;
+    const bool angle = !ede && (cm & kTruthAngle) != 0;
     mpf_init2(dc_re, wp); mpf_set_ui(dc_re, 1);
     mpf_init2(dc_im, wp); mpf_init2(e1, wp); mpf_init2(e2, wp);
     int i = 1;
@@ -546,7 +553,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
         mpf_mul_ui(d_re, d_re, 2);
         mpf_add(d_im, d_im, tt1);
         mpf_mul_ui(d_im, d_im, 2);
-        if (ede) {
+        if (ede || angle) {
             mpf_mul(e1, dc_re, z_im);
             mpf_mul(e2, dc_im, z_re);
             mpf_add(e2, e1, e2);
@@ -570,6 +577,22 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
         double rad = mpf_get_d(tt1);
         if (rad > ESC2) {
             if (nout) *nout = i + 1;
+            if (angle) {
+                // arg z - arg J, J = dz/dc scaled by its larger component (mpf_get_d
+                // of the ratios stays in range whatever the size of J)
+                mpf_abs(e1, dc_re);
+                mpf_abs(e2, dc_im);
+                if (mpf_cmp(e1, e2) < 0) mpf_set(e1, e2);
+                double jr = 0.0, ji = 0.0;
+                if (mpf_sgn(e1) != 0) {
+                    mpf_div(e2, dc_re, e1);
+                    jr = mpf_get_d(e2);
+                    mpf_div(e2, dc_im, e1);
+                    ji = mpf_get_d(e2);
+                }
+                res = (float)(std::atan2(mpf_get_d(z_im), mpf_get_d(z_re)) - std::atan2(ji, jr));
+                break;
+            }
             if (ede) {
                 mpf_mul(e1, dc_re, dc_re);
                 mpf_mul(e2, dc_im, dc_im);
@@ -2085,7 +2108,9 @@ void Engine::truth(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int full_
         mpf_div_ui(soff, soff, SUB);
         mpf_add(cim, cim, soff);
         int nn = -1;
-        out[q] = accuratePoint(cre, cim, mxit, cm, &nn);
+        // the normal map's truth is the angle (the reference's point routine
+        // returns the smooth value there)
+        out[q] = accuratePoint(cre, cim, mxit, (cm & CM_NORMAL) && !(cm & CM_EDE) ? (cm | kTruthAngle) : cm, &nn);
         if (nout) nout[q] = nn;
         mpf_clears(cre, cim, off, soff, (mpf_ptr)0);
     }

@@ -65,6 +65,11 @@ def make(label):
 # that forms which differ from the reference's double path on chaotic samples
 # can be compared with it on the same footing (tests/test_gpu_mixed.py).
 CASE_TRUTH = ("c1", "flake", "ticktock", "deep51")
+# DE-coloured parity cases: truth of the distance (EDE and DE-overlay cases:
+# oracle.truth with EDE, the reference's point routine) or of the normal-map
+# angle arg z - arg dz/dc (the oracle's truth extension), for every sample in
+# the reference's getIndex layout.
+DE_CASE_TRUTH = ("c1_ede", "c1_normal", "c1_deovl_ss3", "minibrot875_ede", "minibrot875_normal", "exterior1000_deovl", "exterior1000_normal")
 
 
 def case_path(name):
@@ -75,19 +80,23 @@ def make_case(name):
     import json
 
     c = json.load(open(os.path.join(HERE, "cases.json")))[name]
-    W, H = c["width"], c["height"]
-    rows, cols = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
-    keys = np.stack([rows.ravel(), cols.ravel(), np.zeros(W * H, int), np.zeros(W * H, int)], axis=1)
+    W, H, sub = c["width"], c["height"], c["sub"]
+    # every sample in getIndex order: sample row y = row sub + sub/2 + subrow
+    ys, xs = np.meshgrid(np.arange(H * sub), np.arange(W * sub), indexing="ij")
+    ys, xs = ys.ravel(), xs.ravel()
+    keys = np.stack([ys // sub, xs // sub, ys % sub - sub // 2, xs % sub - sub // 2], axis=1)
+    cm = c["coloring_method"] & (2 | 16 | 64)
+    cm = 2 if cm & (2 | 64) else cm  # distance truth for EDE and the DE overlay
     t = time.time()
-    tv, tn = oracle.truth(c["center_re"], c["center_im"], c["scale"], W, H, c["max_iterations"], keys, sub=c["sub"], coloring_method=c["coloring_method"], bailout=c["bailout"], threads=os.cpu_count())
+    tv, tn = oracle.truth(c["center_re"], c["center_im"], c["scale"], W, H, c["max_iterations"], keys, sub=sub, coloring_method=cm, bailout=c["bailout"], threads=os.cpu_count())
     np.savez_compressed(case_path(name), N=tn.astype(np.int32), value=tv.astype(np.float32))
-    print("%s: %d samples in %.0f s, %d interior" % (name, W * H, time.time() - t, int(np.sum(tn < 0))))
+    print("%s: %d samples in %.0f s, %d interior" % (name, keys.shape[0], time.time() - t, int(np.sum(tn < 0))))
 
 
 if __name__ == "__main__":
     args = sys.argv[1:]
     if args and args[0] == "--cases":
-        for name in args[1:] or CASE_TRUTH:
+        for name in args[1:] or (CASE_TRUTH + DE_CASE_TRUTH):
             make_case(name)
     else:
         for label in args or views.TRUTH_FRAMES:
