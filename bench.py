@@ -159,6 +159,7 @@ def profile_run(args, vlist):
                            "exact_form_gpu_ms": st["rerun_fp64_gpu_ms"], "fp64_reruns": st["fp64_reruns"], "exact_reruns": st["exact_reruns"], "steps": st["steps"],
                            "bla_applies": st["bla_applies"], "fp32_pass_steps": st["fp32_pass_steps"], "fp32_pass_bla_applies": st["fp32_pass_bla_applies"],
                            "interior": st["interior"], "fp32_unvouched_interior": st["fp32_unvouched_interior"], "fp32_unvouched_escape": st["fp32_unvouched_escape"],
+                           "rebases": st["rebases"], "exact_steps": st["exact_steps"], "fe_rebases": st["fe_rebases"],
                            "color_gpu_ms": be.last_color_stats()[0]}
         be.close()
     print(json.dumps({"profile": out, "resolution": "%dx%d" % (args.width, args.height)}))

@@ -192,9 +192,11 @@ def test_mixed_de_colourings(backend):
     normal map) in mixed precision against arbitrary-precision truth: class
     agreement, 99.9 % of the escape iterations equal to the truth's, and the
     distance (or the normal-map angle) within the stated bounds on the samples
-    whose N agree. The exact form's distances to the same truth are printed
-    beside them: on minibrot875 the reference's FP64 derivative is off by up
-    to 14 % on a few samples where the mixed form is within 1e-7."""
+    whose N agree, or no worse than the exact form where the exact form itself
+    misses them (samples no lane tier can vouch for finish in the exact form).
+    The exact form's distances to the same truth are printed beside them: on
+    minibrot875 the reference's FP64 derivative is off by up to 14 % on a few
+    samples where the mixed form's lanes are within 1e-7."""
     from conftest import GOLDEN
 
     cases = load_cases()
@@ -224,12 +226,13 @@ def test_mixed_de_colourings(backend):
             mv, ev = mi, ei
         else:
             mv, ev = mnr, enr
-        # the reference pixel: its distance / angle is 0 in the reference's
-        # algorithm (its value comes from the reference orbit), in both forms
+        # samples whose distance / angle both forms leave at 0: the reference
+        # pixel (its value comes from the reference orbit) and, under adaptive
+        # supersampling, the sub-samples of pixels that were not flagged
         refpix = None
         if not (cm & 2):
             refpix = (mv == 0) & (ev == 0) & (tv != 0)
-            assert refpix.sum() <= 1, name
+            assert c["sub"] > 1 or refpix.sum() <= 1, name
         mp, mmax, cnt = _de_errors(mv, mn, tv, tn, angle, refpix)
         ep, emax, _ = _de_errors(ev, en, tv, tn, angle, refpix)
         what = "angle |d|" if angle else "|dDE|/DE"
@@ -237,7 +240,9 @@ def test_mixed_de_colourings(backend):
               % (name, same_n, cls, what, mp, mmax, cnt, ep, emax, mst["fp64_reruns"], mi.size))
         assert cls == 0, name
         assert same_n >= 0.999, name
-        assert mp <= (ANGLE_P999 if angle else DE_REL_P999), name
-        assert mmax <= (ANGLE_MAX if angle else DE_REL_MAX), name
+        # within the bounds, or no worse than the exact form where the exact
+        # form itself misses them (its samples are the mixed form's last tier)
+        assert mp <= max(ANGLE_P999 if angle else DE_REL_P999, ep), name
+        assert mmax <= max(ANGLE_MAX if angle else DE_REL_MAX, emax), name
         seen += 1
     assert seen >= 7
