@@ -757,20 +757,26 @@ MBX_HD void lane_j_advance(Lane<T>& L) {
 
 // Common iterations of the FP32 lane without interior detection: iterations
 // that take none of the general code's branches (no BLA skip, orbit entry in
-// range, no escape screen, precision cap, rescale, rebase candidate or end of
-// the reference) are the step, the error update and the index advance. They
-// run here in runs whose length is fixed once per run — up to the next BLA
-// position, the wrap of a periodic orbit, maxiter or the end of the reference,
-// and the call's budget — so that a step carries no index tests; the first
-// iteration that could take a branch is left uncommitted for the general code,
-// which redoes it from the same state with the same operations; a rescale
-// (|w|^2 out of its window) is done in place, exactly as the general code does
-// it (lane_rescale_pow2). Per step: one
-// 16-byte load of {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X +
-// 2 s w' as one paired FMA (so |2 z|^2 is the next error amplification g2 =
-// 4 |z|^2 exactly) and five compares. At a BLA position the per-position
-// radius maximum decides: |dz|^2 not below it fails every level, so the
-// iteration is a common one. Returns the steps taken.
+// range, no escape screen, precision cap, rebase candidate or end of the
+// reference) are the step, the error update and the index advance. They run
+// here in runs of at most kRun steps whose length is fixed once per run — up to
+// the next BLA position, the wrap of a periodic orbit, maxiter or the end of the
+// reference, and the call's budget — each run unrolled, so that a step carries
+// no index arithmetic; the first iteration that could take a branch is left
+// uncommitted for the general code, which redoes it from the same state with
+// the same operations. Rescales (|w|^2 out of its window) are exact powers of
+// two (lane_rescale_pow2), which commute with the step's roundings (every term
+// of w' = (2 X + s w) w + d scales by the same power of two, as do 2 z and the
+// error estimate), so they are taken at the end of a run, a step only guarding
+// |w|^2 against leaving FP32's range. Per step: one 16-byte load of
+// {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X + 2 s w' as one
+// paired FMA (so |2 z|^2 is the next error amplification g2 = 4 |z|^2
+// exactly) and four compares. At a BLA position the per-position radius
+// maximum decides: |dz|^2 not below it fails every level, so the iteration is
+// a common one. Returns the steps taken.
+constexpr int kRun = 8;
+constexpr float kWGuard = 1e30f; // |w|^2 bound of a step between rescales (FP32 range with margin)
+
 template <bool DERIV>
 MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const MixedParams& p, int reflen, bool bla_on, int minlevel, const BlaMaxR2* bmax) {
     using R = LaneReal<float>;
@@ -799,11 +805,33 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
         z2pr = fmaf(s + s, wr, X2.x);
         z2pi = fmaf(s + s, wi, X2.y);
     }
+    float wm2 = fmaf(wr, wr, wi * wi);
     for (;;) {
+        // the window, at the end of the previous run (a power-of-two rescale
+        // commutes with the steps' roundings)
+        if (!(wm2 <= wmax2 && wm2 >= wmin2) && wm2 >= R::kWFloor) {
+            L.wr = wr;
+            L.wi = wi;
+            L.err2 = err2;
+            lane_rescale_pow2(L, wm2);
+            wr = L.wr;
+            wi = L.wi;
+            err2 = L.err2;
+            s = L.s;
+            dr = L.dr;
+            di = L.di;
+            s2x5 = 5.0001f * (s * s);
+            wm2 = fmaf(wr, wr, wi * wi);
+#ifdef __CUDA_ARCH__
+            ss = make_float2(s, s);
+            ss2 = make_float2(s + s, s + s);
+#endif
+        }
         if (m >= mlim) break;
         // the current orbit entry below the lane's range (also X = 0 after a rebase)
         if (fabsf(X2.x) < 2.0f * R::kTinyX && fabsf(X2.y) < 2.0f * R::kTinyX) break;
         int seg = mlim - m;
+        if (seg > kRun) seg = kRun;
         int nidx = rm + 1;
         if (per) {
             if (nidx == per) nidx = 0;
@@ -815,9 +843,8 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
                 if (!bmax) break;
                 const BlaMaxR2 r = bmax[(rm - 1) >> minlevel];
                 if (r.m != 0.0f) {
-                    const float wc2 = R::zabs2(wr, wi);
-                    if (wc2 == 0.0f) break;
-                    const F32E dz2 = te_norm(L.S.m * L.S.m * wc2, 2 * L.S.e); // as lane_bla forms it
+                    if (wm2 == 0.0f) break;
+                    const F32E dz2 = te_norm(L.S.m * L.S.m * wm2, 2 * L.S.e); // as lane_bla forms it
                     if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) break;
                 }
             }
@@ -825,9 +852,57 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
             if (to_next < seg) seg = to_next;
         }
         const float4* qp = q + nidx;
+        if (!DERIV && seg == kRun) {
+            // a full run, speculatively: the kRun steps from the run's start
+            // state with one flag for "every step common", committed at once;
+            // a rare step (about one in fifty) sends the run to the careful
+            // loop below, which redoes it from the same start state
+            float tr = wr, ti = wi, te = err2, tg = g2, tw = wm2;
+            float2 tX = X2;
+            bool ok = true;
+#pragma unroll
+            for (int kk = 0; kk < kRun; ++kk) {
+                const float4 Xn = qp[kk];
+#ifdef __CUDA_ARCH__
+                const float2 f = __ffma2_rn(ss, make_float2(tr, ti), tX);
+#else
+                const float2 f = make_float2(fmaf(s, tr, tX.x), fmaf(s, ti, tX.y));
+#endif
+                const float nwr = fmaf(f.x, tr, fmaf(-f.y, ti, dr));
+                const float nwi = fmaf(f.x, ti, fmaf(f.y, tr, di));
+#ifdef __CUDA_ARCH__
+                const float2 z2 = __ffma2_rn(ss2, make_float2(nwr, nwi), make_float2(Xn.x, Xn.y));
+#else
+                const float2 z2 = make_float2(fmaf(s + s, nwr, Xn.x), fmaf(s + s, nwi, Xn.y));
+#endif
+                const float g2n = fmaf(z2.x, z2.x, z2.y * z2.y);
+                const float nwm2 = fmaf(nwr, nwr, nwi * nwi);
+                const float ne = fmaf(te, tg, R::kEps2 * nwm2);
+                ok = ok & (!(g2n > e4) & (ne <= kLaneCap2 * nwm2) & (nwm2 >= R::kWFloor) & (nwm2 <= kWGuard) & (s2x5 * nwm2 < Xn.z));
+                tr = nwr;
+                ti = nwi;
+                te = ne;
+                tg = g2n;
+                tw = nwm2;
+                tX = make_float2(Xn.x, Xn.y);
+            }
+            if (ok) {
+                wr = tr;
+                wi = ti;
+                err2 = te;
+                g2 = tg;
+                wm2 = tw;
+                X2 = tX;
+                m += kRun;
+                rm = nidx + kRun - 1;
+                continue;
+            }
+        }
         int k = 0;
-        for (; k < seg; ++k) {
-            const float4 Xn = qp[k];
+#pragma unroll
+        for (int kk = 0; kk < kRun; ++kk) {
+            if (kk >= seg) break;
+            const float4 Xn = qp[kk];
 #ifdef __CUDA_ARCH__
             const float2 f = __ffma2_rn(ss, make_float2(wr, wi), X2);
 #else
@@ -841,45 +916,38 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
             const float2 z2 = make_float2(fmaf(s + s, nwr, Xn.x), fmaf(s + s, nwi, Xn.y));
 #endif
             const float g2n = fmaf(z2.x, z2.x, z2.y * z2.y);
-            const float wm2 = fmaf(nwr, nwr, nwi * nwi);
-            const float ne = fmaf(err2, g2, R::kEps2 * wm2);
+            const float nwm2 = fmaf(nwr, nwr, nwi * nwi);
+            const float ne = fmaf(err2, g2, R::kEps2 * nwm2);
             // (|w| = 0 and the precision cap both leave through the |w|^2
             // tests; a NaN fails them too)
-            const bool common = !(g2n > e4) && ne <= kLaneCap2 * wm2 && wm2 >= R::kWFloor && s2x5 * wm2 < Xn.z;
+            const bool common = !(g2n > e4) && ne <= kLaneCap2 * nwm2 && nwm2 >= R::kWFloor && nwm2 <= kWGuard && s2x5 * nwm2 < Xn.z;
             if (!common) break;
             wr = nwr;
             wi = nwi;
             err2 = ne;
             g2 = g2n;
+            wm2 = nwm2;
             X2 = make_float2(Xn.x, Xn.y);
             if (DERIV) {
                 lane_j_step_2z(L, z2pr, z2pi);
-                z2pr = z2.x; // (a rescale below leaves 2 s w unchanged)
+                z2pr = z2.x;
                 z2pi = z2.y;
             }
-            if (!(wm2 <= wmax2 && wm2 >= wmin2)) {
-                // |w| left the window: the general code's rescale, in place
-                // (the rebase screen above is invariant under it)
-                L.wr = wr;
-                L.wi = wi;
-                L.err2 = err2;
-                lane_rescale_pow2(L, wm2);
-                wr = L.wr;
-                wi = L.wi;
-                err2 = L.err2;
-                s = L.s;
-                dr = L.dr;
-                di = L.di;
-                s2x5 = 5.0001f * (s * s);
-#ifdef __CUDA_ARCH__
-                ss = make_float2(s, s);
-                ss2 = make_float2(s + s, s + s);
-#endif
-            }
+            k = kk + 1;
         }
         m += k;
         if (k > 0) rm = nidx + k - 1;
-        if (k < seg) break; // a rare iteration: the general code takes it
+        if (k < seg) break; // a rare iteration: the general code takes it (after the window below)
+    }
+    // leave with |w|^2 inside the window, as the general code keeps it
+    if (!(wm2 <= wmax2 && wm2 >= wmin2) && wm2 >= R::kWFloor) {
+        L.wr = wr;
+        L.wi = wi;
+        L.err2 = err2;
+        lane_rescale_pow2(L, wm2);
+        wr = L.wr;
+        wi = L.wi;
+        err2 = L.err2;
     }
     L.wr = wr;
     L.wi = wi;

@@ -231,7 +231,7 @@ def test_mixed_de_colourings(backend):
         # supersampling, the sub-samples of pixels that were not flagged
         refpix = None
         if not (cm & 2):
-            refpix = (mv == 0) & (ev == 0) & (tv != 0)
+            refpix = (mv == 0) & (ev == 0) & (tv != 0) & (tn > 0)
             assert c["sub"] > 1 or refpix.sum() <= 1, name
         mp, mmax, cnt = _de_errors(mv, mn, tv, tn, angle, refpix)
         ep, emax, _ = _de_errors(ev, en, tv, tn, angle, refpix)
