@@ -755,82 +755,158 @@ MBX_HD void lane_j_advance(Lane<T>& L) {
 }
 
 
-// Common iterations of the FP32 lane without interior detection: iterations
-// that take none of the general code's branches (no BLA skip, orbit entry in
-// range, no escape screen, precision cap, rebase candidate or end of the
-// reference) are the step, the error update and the index advance. They run
-// here in runs of at most kRun steps whose length is fixed once per run — up to
-// the next BLA position, the wrap of a periodic orbit, maxiter or the end of the
-// reference, and the call's budget — each run unrolled, so that a step carries
-// no index arithmetic; the first iteration that could take a branch is left
-// uncommitted for the general code, which redoes it from the same state with
-// the same operations. Rescales (|w|^2 out of its window) are exact powers of
-// two (lane_rescale_pow2), which commute with the step's roundings (every term
-// of w' = (2 X + s w) w + d scales by the same power of two, as do 2 z and the
-// error estimate), so they are taken at the end of a run, a step only guarding
-// |w|^2 against leaving FP32's range. Per step: one 16-byte load of
-// {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X + 2 s w' as one
-// paired FMA (so |2 z|^2 is the next error amplification g2 = 4 |z|^2
+// The general code's rebase decision on a post-step state (mp.cpp:3584-3615):
+// 0 none, 1 rebase in the lane type, 2 the floatexp decision. |z|^2 < |dz|^2 is
+// decided on floatexp with a 1e-4 margin; inside the margin, for strong
+// cancellation in X + dz, and at the end of the reference it is left to
+// floatexp. Screen: |dz|^2 < |X|^2 / 5 means |z| > |dz| (no rebase); s = 0 when
+// S is below the type's range, where |dz|^2 <= 2^-252 wmax2 is far below any
+// |X|^2 above kTinyX^2.
+template <class T>
+MBX_HD int lane_rebase_decision(const TE<T>& S, T s, T wr, T wi, typename LaneReal<T>::V2 Xc, int m, typename LaneReal<T>::Z zrad, int per, int reflen) {
+    using R = LaneReal<T>;
+    using Z = typename R::Z;
+    if (!per && m >= reflen) return 2;
+    const Z w2 = R::zabs2(wr, wi);
+    const Z xr2 = R::zabs2(Xc.x, Xc.y);
+    const Z sz = R::z(s);
+    if (xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * w2 < Z(0.2) * xr2) return 0;
+    const TE<Z> dz2 = te_norm(R::z(S.m) * R::z(S.m) * w2, 2 * S.e);
+    if (dz2.m == Z(0)) return 0;
+    if (zrad == Z(0)) return 2;
+    // q = |z|^2 / |dz|^2 against 1 -/+ 1e-4 without a division:
+    // z2.m 2^(z2.e - dz2.e) against dz2.m (1 -/+ 1e-4)
+    const TE<Z> z2 = te_norm(zrad, 0);
+    const Z zq = ldexp_ftz(z2.m, imax(-R::kExpClamp, imin(R::kExpClamp, z2.e - dz2.e)));
+    if (zq < Z(0.9999) * dz2.m) return (zrad > Z(0.25) * xr2 && s != T(0)) ? 1 : 2;
+    if (zq < Z(1.0001) * dz2.m) return 2;
+    return 0;
+}
+
+// Decision 1: the delta restarts as dz = z from the start of the reference;
+// the error estimate changes units (S_old / S_new)^2 and gains one rounding.
+template <class T>
+MBX_HD void lane_rebase_to(Lane<T>& L, T zr, T zi) {
+    using R = LaneReal<T>;
+    const TE<T> S0 = L.S;
+    lane_set_delta(L, zr, zi, 0);
+    lane_refresh(L);
+    if (R::kTrackError) L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2;
+    L.m = 0;
+    L.rm = -1;
+    L.Xc = R::make2(T(0), T(0));
+}
+
+// Common iterations of the FP32 lane without interior detection. The
+// iterations that take none of the general code's rare branches (orbit entry
+// below range, escape screen, precision cap, the floatexp rebase decision, end
+// of the reference) run here, and so do its two frequent ones — a BLA skip at a
+// BLA position and a rebase the general code takes in the lane type — through
+// the same helpers (lane_bla, lane_rebase_decision, lane_rebase_to), so that a
+// sample's result does not depend on which of the two paths took an
+// iteration. The first iteration that could take another branch is left
+// uncommitted for the general code, which redoes it from the same state.
+//
+// Steps run in runs of at most kRun whose length is fixed once per run (up to
+// the next BLA position, the wrap of a periodic orbit, maxiter or the end of
+// the reference, and the call's budget). A full run is computed speculatively
+// — kRun steps from the run's start state, unrolled, with one flag for "every
+// step common" — and committed at once; a rare step in it (about one in fifty)
+// sends the run to the careful loop, which redoes it one step at a time.
+// Rescales (|w|^2 out of its window) are exact powers of two
+// (lane_rescale_pow2), which commute with the step's roundings (every term of
+// w' = (2 X + s w) w + d scales by the same power of two, as do 2 z, the error
+// estimate and the BLA and rebase decisions), so they are taken between runs, a
+// step only guarding |w|^2 against leaving FP32's range. Per step: one 16-byte
+// load of {2 X, |X|^2 or 0} (MixedParams::Zq), the step, 2 z = 2 X + 2 s w' as
+// one paired FMA (so |2 z|^2 is the next error amplification g2 = 4 |z|^2
 // exactly) and four compares. At a BLA position the per-position radius
-// maximum decides: |dz|^2 not below it fails every level, so the iteration is
-// a common one. Returns the steps taken.
+// maximum screens: |dz|^2 not below it fails every level. Returns the budget
+// used (a step or a BLA skip counts one); the counters are the lane pass's.
 constexpr int kRun = 8;
 constexpr float kWGuard = 1e30f; // |w|^2 bound of a step between rescales (FP32 range with margin)
 
 template <bool DERIV>
-MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const MixedParams& p, int reflen, bool bla_on, int minlevel, const BlaMaxR2* bmax) {
+MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const MixedParams& p, const BlaView& bv, const Bla32* blat, const float2* orb, int reflen,
+                          unsigned& n_steps, unsigned& n_bla, unsigned long long& n_skip, unsigned& n_rebase) {
     using R = LaneReal<float>;
     const float4* q = p.Zq;
     const int per = p.per;
-    const int m0 = L.m, off = L.iter - L.m;
-    int mlim = g.mxit - off; // m reaching mlim: maxiter, or the end of a non-periodic reference
-    if (!per && reflen - 1 < mlim) mlim = reflen - 1;
-    if (m0 + budget < mlim) mlim = m0 + budget;
-    float s = L.s;
-    float s2x5 = 5.0001f * (s * s); // |dz|^2 < |X|^2 / 5 as 5.0001 s^2 |w|^2 < |X|^2 (implies the general code's rebase screen)
-    const float e4 = 4.0f * p.esc2lo;     // |2 z|^2 > 4 ESC2lo: the escape screen on 4 |z|^2 (exact scaling)
+    const BlaMaxR2* bmax = p.blamax;
+    const int minlevel = bv.minlevel;
+    const bool bla_on = blat != nullptr;
+    int left = budget;
+    const float e4 = 4.0f * p.esc2lo; // |2 z|^2 > 4 ESC2lo: the escape screen on 4 |z|^2 (exact scaling)
     const float wmax2 = p.wmax2, wmin2 = p.wmin2;
     const int blamask = (1 << minlevel) - 1;
+    float s = L.s, dr = L.dr, di = L.di;
+    float s2x5 = 5.0001f * (s * s); // |dz|^2 < |X|^2 / 5 as 5.0001 s^2 |w|^2 < |X|^2 (implies the general code's rebase screen)
     float wr = L.wr, wi = L.wi;
-    float dr = L.dr, di = L.di;
     float err2 = L.err2, g2 = L.g2;
     float2 X2 = make_float2(L.Xc.x + L.Xc.x, L.Xc.y + L.Xc.y);
-    int m = m0, rm = L.rm;
+    int m = L.m, rm = L.rm, it = L.iter; // it: the iteration count (a rebase restarts m, not it)
 #ifdef __CUDA_ARCH__
     float2 ss = make_float2(s, s), ss2 = make_float2(s + s, s + s);
 #endif
     // DE: 2 z before the step, for J' = 2 z J + 1 (the general code's form)
     float z2pr = 0.0f, z2pi = 0.0f;
+    float wm2 = fmaf(wr, wr, wi * wi);
+    // the lane's state into L and back (around the shared helpers)
+    auto sync_out = [&]() {
+        L.wr = wr;
+        L.wi = wi;
+        L.err2 = err2;
+        L.g2 = g2;
+        L.m = m;
+        L.iter = it;
+        L.rm = rm;
+        L.Xc = make_float2(0.5f * X2.x, 0.5f * X2.y); // exact
+    };
+    auto sync_in = [&]() {
+        wr = L.wr;
+        wi = L.wi;
+        err2 = L.err2;
+        g2 = L.g2;
+        m = L.m;
+        rm = L.rm;
+        it = L.iter;
+        X2 = make_float2(L.Xc.x + L.Xc.x, L.Xc.y + L.Xc.y);
+        s = L.s;
+        dr = L.dr;
+        di = L.di;
+        s2x5 = 5.0001f * (s * s);
+        wm2 = fmaf(wr, wr, wi * wi);
+#ifdef __CUDA_ARCH__
+        ss = make_float2(s, s);
+        ss2 = make_float2(s + s, s + s);
+#endif
+        if (DERIV) {
+            z2pr = fmaf(s + s, wr, X2.x);
+            z2pi = fmaf(s + s, wi, X2.y);
+        }
+    };
     if (DERIV) {
         z2pr = fmaf(s + s, wr, X2.x);
         z2pi = fmaf(s + s, wi, X2.y);
     }
-    float wm2 = fmaf(wr, wr, wi * wi);
     for (;;) {
-        // the window, at the end of the previous run (a power-of-two rescale
-        // commutes with the steps' roundings)
+        // the window, between runs (a power-of-two rescale commutes with the
+        // steps' roundings)
         if (!(wm2 <= wmax2 && wm2 >= wmin2) && wm2 >= R::kWFloor) {
-            L.wr = wr;
-            L.wi = wi;
-            L.err2 = err2;
+            sync_out();
             lane_rescale_pow2(L, wm2);
-            wr = L.wr;
-            wi = L.wi;
-            err2 = L.err2;
-            s = L.s;
-            dr = L.dr;
-            di = L.di;
-            s2x5 = 5.0001f * (s * s);
-            wm2 = fmaf(wr, wr, wi * wi);
-#ifdef __CUDA_ARCH__
-            ss = make_float2(s, s);
-            ss2 = make_float2(s + s, s + s);
-#endif
+            sync_in();
         }
-        if (m >= mlim) break;
-        // the current orbit entry below the lane's range (also X = 0 after a rebase)
-        if (fabsf(X2.x) < 2.0f * R::kTinyX && fabsf(X2.y) < 2.0f * R::kTinyX) break;
-        int seg = mlim - m;
+        // maxiter, or the end of a non-periodic reference (where the general
+        // code forces the rebase)
+        int seg = g.mxit - it;
+        if (!per && reflen - 1 - m < seg) seg = reflen - 1 - m;
+        if (seg <= 0 || left <= 0) break;
+        // (the budget is a soft bound: a run is not cut by it, so that runs stay
+        // full and aligned to the BLA positions; a call overshoots by < kRun)
+        // the current orbit entry below the lane's range (X = 0 after a rebase
+        // takes a common step when s is a normal number well above FP32's floor)
+        if (m == 0 ? !(s >= R::kMinS) : (fabsf(X2.x) < 2.0f * R::kTinyX && fabsf(X2.y) < 2.0f * R::kTinyX)) break;
         if (seg > kRun) seg = kRun;
         int nidx = rm + 1;
         if (per) {
@@ -845,7 +921,31 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
                 if (r.m != 0.0f) {
                     if (wm2 == 0.0f) break;
                     const F32E dz2 = te_norm(L.S.m * L.S.m * wm2, 2 * L.S.e); // as lane_bla forms it
-                    if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) break;
+                    if (dz2.e < r.e || (dz2.e == r.e && dz2.m < r.m)) {
+                        // a level may apply: the general code's BLA attempt
+                        sync_out();
+                        float amp2 = 0.0f;
+                        BlaEntry<float> used;
+                        const int skip = lane_bla(bv, blat, orb, per > 0, rm, L.S, L.wr, L.wi, L.dcm, L.dce, p.esc2lo, per ? per : reflen, amp2, DERIV ? &used : nullptr);
+                        if (skip > 0) {
+                            ++n_bla;
+                            n_skip += (unsigned long long)skip;
+                            --left;
+                            L.m += skip;
+                            L.iter += skip;
+                            L.rm += skip;
+                            if (per && L.rm >= per) L.rm -= per;
+                            lane_refresh(L);
+                            L.Xc = orb[L.rm];
+                            // the skip carries the error by A; |w| is 1 afterwards
+                            L.err2 = L.err2 * amp2 + R::kEps2;
+                            L.g2 = 4.0f * lane_abs2f(L.Xc);
+                            if (DERIV) lane_j_bla(L, used);
+                            sync_in();
+                            continue;
+                        }
+                        // no level applies: a common iteration
+                    }
                 }
             }
             const int to_next = blamask + 1 - u; // iterations to the next BLA position
@@ -853,10 +953,7 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
         }
         const float4* qp = q + nidx;
         if (!DERIV && seg == kRun) {
-            // a full run, speculatively: the kRun steps from the run's start
-            // state with one flag for "every step common", committed at once;
-            // a rare step (about one in fifty) sends the run to the careful
-            // loop below, which redoes it from the same start state
+            // a full run, speculatively (see above)
             float tr = wr, ti = wi, te = err2, tg = g2, tw = wm2;
             float2 tX = X2;
             bool ok = true;
@@ -894,15 +991,19 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
                 wm2 = tw;
                 X2 = tX;
                 m += kRun;
+                it += kRun;
                 rm = nidx + kRun - 1;
+                left -= kRun;
+                n_steps += kRun;
                 continue;
             }
         }
-        int k = 0;
-#pragma unroll
-        for (int kk = 0; kk < kRun; ++kk) {
-            if (kk >= seg) break;
-            const float4 Xn = qp[kk];
+        // the careful loop: one step at a time up to the run's end or its first
+        // rare step; a rebase the general code would take in the lane type is
+        // taken here
+        bool leave = false, rebased = false;
+        for (int k = 0; k < seg; ++k) {
+            const float4 Xn = qp[k];
 #ifdef __CUDA_ARCH__
             const float2 f = __ffma2_rn(ss, make_float2(wr, wi), X2);
 #else
@@ -920,44 +1021,59 @@ MBX_HDF int lane_fast_f32(Lane<float>& L, int budget, const FrameGeom& g, const 
             const float ne = fmaf(err2, g2, R::kEps2 * nwm2);
             // (|w| = 0 and the precision cap both leave through the |w|^2
             // tests; a NaN fails them too)
-            const bool common = !(g2n > e4) && ne <= kLaneCap2 * nwm2 && nwm2 >= R::kWFloor && nwm2 <= kWGuard && s2x5 * nwm2 < Xn.z;
-            if (!common) break;
+            const bool others = !(g2n > e4) && ne <= kLaneCap2 * nwm2 && nwm2 >= R::kWFloor && nwm2 <= kWGuard;
+            if (!others) {
+                leave = true;
+                break;
+            }
+            int decide = 0;
+            if (!(s2x5 * nwm2 < Xn.z)) {
+                // the rebase screen: the general code's decision on the
+                // post-step state (z = 2 z / 2 exactly)
+                const float zr = 0.5f * z2.x, zi = 0.5f * z2.y;
+                decide = lane_rebase_decision<float>(L.S, s, nwr, nwi, make_float2(0.5f * Xn.x, 0.5f * Xn.y), m + 1, fmaf(zr, zr, zi * zi), per, reflen);
+                if (decide == 2) {
+                    leave = true;
+                    break;
+                }
+            }
+            // commit the step
+            if (DERIV) {
+                lane_j_step_2z(L, z2pr, z2pi);
+                z2pr = z2.x;
+                z2pi = z2.y;
+            }
             wr = nwr;
             wi = nwi;
             err2 = ne;
             g2 = g2n;
             wm2 = nwm2;
             X2 = make_float2(Xn.x, Xn.y);
-            if (DERIV) {
-                lane_j_step_2z(L, z2pr, z2pi);
-                z2pr = z2.x;
-                z2pi = z2.y;
+            ++m;
+            ++it;
+            rm = nidx + k;
+            --left;
+            ++n_steps;
+            if (decide == 1) {
+                sync_out();
+                lane_rebase_to(L, 0.5f * z2.x, 0.5f * z2.y);
+                ++n_rebase;
+                sync_in();
+                rebased = true;
+                break;
             }
-            k = kk + 1;
         }
-        m += k;
-        if (k > 0) rm = nidx + k - 1;
-        if (k < seg) break; // a rare iteration: the general code takes it (after the window below)
+        if (leave) break; // a rare iteration: the general code takes it (after the window below)
+        (void)rebased;
     }
     // leave with |w|^2 inside the window, as the general code keeps it
     if (!(wm2 <= wmax2 && wm2 >= wmin2) && wm2 >= R::kWFloor) {
-        L.wr = wr;
-        L.wi = wi;
-        L.err2 = err2;
+        sync_out();
         lane_rescale_pow2(L, wm2);
-        wr = L.wr;
-        wi = L.wi;
-        err2 = L.err2;
+        sync_in();
     }
-    L.wr = wr;
-    L.wi = wi;
-    L.err2 = err2;
-    L.g2 = g2;
-    L.m = m;
-    L.iter = m + off;
-    L.rm = rm;
-    L.Xc = make_float2(0.5f * X2.x, 0.5f * X2.y); // exact
-    return m - m0;
+    sync_out();
+    return budget - left;
 }
 
 // Interior decision: a lane whose error estimate is too large leaves for the
@@ -996,10 +1112,9 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
     for (int b = 0; b < budget; ++b) {
         if constexpr (std::is_same<T, float>::value && !FASTI) {
             if (!(INTR && p.use_interior) && p.Zq) {
-                const int took = deriv ? lane_fast_f32<true>(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax)
-                                       : lane_fast_f32<false>(L, budget - b, g, p, reflen, blat != nullptr, f.bla.minlevel, p.blamax);
-                n_steps += (unsigned)took;
-                b += took;
+                const int used = deriv ? lane_fast_f32<true>(L, budget - b, g, p, f.bla, blat, orb, reflen, n_steps, n_bla, n_skip, n_rebase)
+                                       : lane_fast_f32<false>(L, budget - b, g, p, f.bla, blat, orb, reflen, n_steps, n_bla, n_skip, n_rebase);
+                b += used;
                 if (b >= budget) return 0;
             }
         }
@@ -1304,35 +1419,10 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         // Rebase (mp.cpp:3584-3615): |z|^2 < |dz|^2 decided on floatexp with a
         // 1e-4 margin; FP64 floatexp inside the margin, for strong
         // cancellation in X + dz, and at the end of the reference.
-        const Z w2 = R::zabs2(L.wr, L.wi);
-        int decide = 0; // 0 none, 1 rebase in the lane type, 2 FP64 floatexp test
-        // Screen: |dz|^2 < |X|^2 / 5 means |z| > |dz| (no rebase). s = 0 when S
-        // is below the type's range, where |dz|^2 <= 2^-252 wmax2 is far below
-        // any |X|^2 above kTinyX^2.
-        const Z xr2 = R::zabs2(L.Xc.x, L.Xc.y);
-        const Z sz = R::z(L.s);
-        const bool far = xr2 > Z(R::kTinyX) * Z(R::kTinyX) && sz * sz * w2 < Z(0.2) * xr2;
-        const TE<Z> dz2 = far ? TE<Z>{Z(0), 0} : te_norm(R::z(L.S.m) * R::z(L.S.m) * w2, 2 * L.S.e);
-        if (!per && L.m >= reflen) decide = 2;
-        else if (!far && dz2.m != Z(0)) {
-            if (zrad == Z(0)) decide = 2;
-            else {
-                // q = |z|^2 / |dz|^2 compared with 1 -/+ 1e-4 without a division:
-                // z2.m 2^(z2.e - dz2.e) against dz2.m (1 -/+ 1e-4)
-                const TE<Z> z2 = te_norm(zrad, 0);
-                const Z zq = ldexp_ftz(z2.m, imax(-R::kExpClamp, imin(R::kExpClamp, z2.e - dz2.e)));
-                if (zq < Z(0.9999) * dz2.m) decide = (zrad > Z(0.25) * xr2 && L.s != T(0)) ? 1 : 2;
-                else if (zq < Z(1.0001) * dz2.m) decide = 2;
-            }
-        }
+        const int decide = lane_rebase_decision<T>(L.S, L.s, L.wr, L.wi, L.Xc, L.m, zrad, per, reflen);
         const TE<T> S0 = L.S;
         if (decide == 1) {
-            lane_set_delta(L, zr, zi, 0);
-            lane_refresh(L);
-            if (R::kTrackError) L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2;
-            L.m = 0;
-            L.rm = -1;
-            L.Xc = R::make2(T(0), T(0));
+            lane_rebase_to(L, zr, zi);
             ++n_rebase;
         } else if (decide == 2 && std::is_same<T, float>::value) {
             // the decision and the new delta in FP32 floatexp: z = X + S w
