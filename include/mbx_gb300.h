@@ -70,6 +70,17 @@ typedef struct {
                                   fixed c below (compute_backend.cpp:268); precision_mode does not apply */
     const char* fixed_c_re;    /* Julia: fixed c, decimal (ComputeRequest::fixedCRe / fixedCIm) */
     const char* fixed_c_im;
+    /* Optional periodic reference (no reference counterpart; the reference finds a
+     * nucleus per frame, mp.cpp:1227-1386): with reference_period > 0 the frame's
+     * reference is the given nucleus of that period, used whatever its size in
+     * the frame, and its one-period orbit is kept on the context, so that every
+     * frame of a zoom sequence toward it (the same nucleus, period and
+     * precision_bits) reuses the orbit; only the per-frame parts (its position
+     * in the frame, the BLA table for the frame's radius) are redone. Perturbation
+     * frames (scale > 1e6) only. */
+    const char* reference_re;
+    const char* reference_im;
+    int reference_period;
 } mbx_request;
 
 typedef struct {

@@ -47,6 +47,8 @@ int validate(const mbx_request* r, std::string& why) {
     else if (!(r->bailout >= 0.0) || r->bailout > 1e18) why = "bailout must be in [0, 1e18]";
     else if ((long long)r->width * r->sub * r->height * r->sub > (1ll << 31) - 1) why = "frame too large";
     else if (r->height >= (1 << 24) || r->width >= (1 << 24)) why = "dimensions too large";
+    else if (r->reference_period < 0 || (r->reference_period > 0 && (!r->reference_re || !r->reference_im || r->compute_mode != MBX_MODE_MANDELBROT)))
+        why = "a periodic reference needs its nucleus (reference_re, reference_im), a period >= 1 and a Mandelbrot frame";
     else return MBX_OK;
     return MBX_E_INVALID;
 }

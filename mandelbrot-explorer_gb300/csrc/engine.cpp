@@ -556,6 +556,7 @@ bool Engine::ref_tail_escapes(int last, int extra) { // mp.cpp:927-957
 // createRef (mp.cpp:4014-4187). `pick` < 0: view centre; otherwise the
 // reference pixel key (already chosen and removed from the pending set).
 int Engine::build_reference(const int* pick, bool view_center) {
+    zoom_valid_ = false; // the orbit shadows are overwritten
     ref_period_ = 0;
     ref_escaped_ = false;
     ref_escape_it_ = 0;
@@ -1095,7 +1096,9 @@ int Engine::find_nucleus(int maxp) { // mp.cpp:1072-1107 (writes the nucleus int
     return mpf_cmp(dist, r) <= 0 ? period : 0;
 }
 
-int Engine::build_periodic_reference(int period) { // mp.cpp:1109-1172
+// The nucleus ref_re_/ref_im_ as the frame's virtual reference: its position in
+// pixel units and the pixel it rounds to (mp.cpp:1109-1125).
+void Engine::periodic_reference_geometry() {
     ref_escaped_ = false;
     ref_escape_it_ = 0;
     ref_virtual_ = true;
@@ -1112,6 +1115,11 @@ int Engine::build_periodic_reference(int period) { // mp.cpp:1109-1172
     ref_[3] = 0;
     ref_frac_re_ = (ref_x_ - px) * mpf_ld(dx_);
     ref_frac_im_ = (ref_y_ - py) * mpf_ld(dy_);
+}
+
+int Engine::build_periodic_reference(int period) { // mp.cpp:1109-1172
+    zoom_valid_ = false; // the orbit shadows are overwritten
+    periodic_reference_geometry();
     mpf_set(zre_[0], ref_re_);
     mpf_set(zim_[0], ref_im_);
     use_fixed_ = false;
@@ -1157,6 +1165,85 @@ FE Engine::nucleus_size() const { // mp.cpp:1195-1219
     FE denom = fe_mul(bmag, fe_mul(lmag, lmag));
     if (denom.m == 0.0) return fe_make(1.0, 1000000);
     return fe_div(fe_make(1.0, 0), denom);
+}
+
+// The request's periodic reference (mbx_request.reference_period > 0; no
+// reference counterpart): the given nucleus is the frame's reference whatever
+// its size in the frame, on the floatexp path. Its one-period orbit is built
+// once and kept (host shadows, device orbit) while the nucleus, period,
+// precision and derivative need stay the same, so the frames of a zoom
+// sequence toward it share it; per frame only the nucleus's position, the BLA
+// table (its validity radii follow the frame's radius) and the mixed form's
+// per-frame tables are redone. The lanes rebase, so one orbit serves every
+// depth.
+int Engine::zoom_reference(int* ref_it) {
+    const int p = zoom_period_;
+    if (mpf_set_str(ref_re_, zoom_re_.c_str(), 10) != 0 || mpf_set_str(ref_im_, zoom_im_.c_str(), 10) != 0) {
+        err_ = "unparsable reference nucleus";
+        return MBX_E_INVALID;
+    }
+    cache_.valid = false; // (the reuse cache and this share the orbit shadows)
+    use_floatexp_ = true;
+    fe_cutoff_sensitive_ = false;
+    ref_subpixel_ = false;
+    ref_value_pending_ = false;
+    periodic_reference_geometry();
+    reset_series();
+    sa_valid_ = false;
+    sa_it_ = 0;
+    sa_order_ = 0;
+    ref_period_ = p;
+    char kb[96];
+    snprintf(kb, sizeof(kb), "|%d|%lu|%d", p, (unsigned long)mpf_get_prec(ref_re_), deriv_ ? 1 : 0);
+    const std::string key = zoom_re_ + "|" + zoom_im_ + kb;
+    if (zoom_valid_ && zoom_key_ == key) {
+        stats_.reused_reference = 1;
+    } else {
+        zoom_valid_ = false;
+        const double t0 = now_ms();
+        hZ_.assign((size_t)p + 2, make_double2(0, 0));
+        hzm3_.assign((size_t)p + 2, 0.0);
+        hD_.assign((size_t)p + 2, make_double2(0, 0));
+        hZfe_.assign((size_t)p + 2, FE2{fe_make(0, 0), fe_make(0, 0)});
+        mpf_set(zre_[0], ref_re_);
+        mpf_set(zim_[0], ref_im_);
+        use_fixed_ = false;
+        hZ_[0] = make_double2(mpf_ld(ref_re_), mpf_ld(ref_im_));
+        hZfe_[0].re = mpf_fe(ref_re_);
+        hZfe_[0].im = mpf_fe(ref_im_);
+        hzm3_[0] = (hZ_[0].x * hZ_[0].x + hZ_[0].y * hZ_[0].y) / 1000000;
+        hD_[0] = make_double2(1.0, 0.0);
+        dfe_r_ = fe_make(1.0, 0);
+        dfe_i_ = fe_make(0.0, 0);
+        {
+            ParSession par(mpf_get_prec(ref_re_) >= kParBits2);
+            for (int i = 1; i < p; ++i) {
+                if (cancel_.load()) return MBX_E_CANCELLED;
+                orbit_step(i, 0, false);
+            }
+        }
+        stats_.orbit_ms += now_ms() - t0;
+        ++stats_.references;
+        const double t1 = now_ms();
+        if (!ensure(dZ_, (size_t)p + 2) || !ensure(dzm3_, (size_t)p + 2) || !ensure(dZfe_, (size_t)p + 2) || (deriv_ && !ensure(dD_, (size_t)p + 2)))
+            return MBX_E_NOMEM;
+        copy_async(dZ_.p, hZ_.data(), sizeof(double2) * p, cudaMemcpyHostToDevice);
+        copy_async(dzm3_.p, hzm3_.data(), sizeof(double) * p, cudaMemcpyHostToDevice);
+        copy_async(dZfe_.p, hZfe_.data(), sizeof(FE2) * p, cudaMemcpyHostToDevice);
+        if (deriv_) copy_async(dD_.p, hD_.data(), sizeof(double2) * p, cudaMemcpyHostToDevice);
+        stats_.copy_ms += now_ms() - t1;
+        const int rc = cuda_ok("orbit upload");
+        if (rc != MBX_OK) return rc;
+        zoom_valid_ = true;
+        zoom_key_ = key;
+    }
+    stats_.reference_length = p;
+    orbit_len_ = p;
+    *ref_it = p;
+    int rc = build_bla(p);
+    if (rc != MBX_OK) return rc;
+    if (mixed_active()) rc = prepare_mixed();
+    return rc;
 }
 
 // buildReferenceOrbit (mp.cpp:1227-1386).
@@ -1907,6 +1994,11 @@ int Engine::compute_frame(const mbx_request& r) {
     cm_ = r.coloring_method;
     mode_ = r.precision_mode;
     deriv_ = (cm_ & (2 | 16 | 64)) != 0; // EDE, normal map, DE overlay (mp.cpp:4190-4192)
+    zoom_period_ = r.reference_period > 0 ? r.reference_period : 0;
+    if (zoom_period_ > 0) {
+        zoom_re_ = r.reference_re;
+        zoom_im_ = r.reference_im;
+    }
     escf_ = (float)(r.bailout > 0 ? r.bailout : 1e8);
     ESC2_ = (double)(escf_ * escf_);
     const int full_h = r.full_height > 0 ? r.full_height : 0;
@@ -2026,9 +2118,13 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     int ref_it = 0;
     int rc = MBX_OK;
     refs_built_in_frame_ = 0;
-    if (reuse_ && restore_cache(&ref_it)) {
+    if (zoom_period_ > 0) {
+        rc = zoom_reference(&ref_it);
+        if (rc != MBX_OK) return rc;
+    } else if (reuse_ && restore_cache(&ref_it)) {
         stats_.reused_reference = 1; // the host orbit shadows still hold this reference
     } else {
+        zoom_valid_ = false; // the orbit shadows are rebuilt below
         // host orbit shadows, up to maxiter + 1 entries (tens of MB at maxiter
         // 1e6): cleared only when a reference is built
         hZ_.assign((size_t)MXIT_ + 2, make_double2(0, 0));

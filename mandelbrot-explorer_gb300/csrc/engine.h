@@ -131,6 +131,8 @@ class Engine {
     int build_reference(const int* pick, bool view_center);
     int find_nucleus(int maxp);
     int build_periodic_reference(int period);
+    void periodic_reference_geometry();
+    int zoom_reference(int* ref_it);
     FE nucleus_size() const;
     int reference_for_frame();
     int upload_reference(int ref_it);
@@ -290,6 +292,11 @@ class Engine {
     } cache_;
     std::string frame_key_;
     bool reuse_ = false;
+    // the request's periodic reference (zoom sequences): nucleus, period, and
+    // whether the orbit shadows hold its orbit (zoom_key_)
+    std::string zoom_re_, zoom_im_, zoom_key_;
+    int zoom_period_ = 0;
+    bool zoom_valid_ = false;
     int refs_built_in_frame_ = 0;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evm_ = nullptr;
     void save_cache(int ref_it);

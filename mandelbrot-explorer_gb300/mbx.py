@@ -66,6 +66,9 @@ class _Request(ctypes.Structure):
         ("compute_mode", ctypes.c_int),
         ("fixed_c_re", ctypes.c_char_p),
         ("fixed_c_im", ctypes.c_char_p),
+        ("reference_re", ctypes.c_char_p),
+        ("reference_im", ctypes.c_char_p),
+        ("reference_period", ctypes.c_int),
     ]
 
 
@@ -300,6 +303,9 @@ class ComputeRequest:
     compute_mode: int = 0  # MODE_MANDELBROT / MODE_JULIA (ComputeMode)
     fixed_c_re: Optional[str] = None  # Julia: the fixed c
     fixed_c_im: Optional[str] = None
+    reference_re: Optional[str] = None  # optional periodic reference (zoom sequences): nucleus and period
+    reference_im: Optional[str] = None
+    reference_period: int = 0
 
     def sample_count(self) -> int:
         return self.width * self.height * self.sub * self.sub
@@ -415,6 +421,9 @@ class CudaComputeBackend:
             req.compute_mode,
             req.fixed_c_re.encode() if req.fixed_c_re is not None else None,
             req.fixed_c_im.encode() if req.fixed_c_im is not None else None,
+            req.reference_re.encode() if req.reference_re is not None else None,
+            req.reference_im.encode() if req.reference_im is not None else None,
+            req.reference_period,
         )
         return r, (req.iterations, req.normal, req.escape_iteration)
 

@@ -123,6 +123,20 @@ def frame(label: str, width: int = 1920, height: int = 1080):
 if __name__ == "__main__":
     import sys
 
+    if "--regenerate-zoom" in sys.argv:
+        import mbx
+
+        d = nucleus()
+        getcontext().prec = len(d["nucleus_re"]) + 40
+        rng = np.random.RandomState(5005)
+        phi = rng.uniform(0, 2 * math.pi)
+        r = Decimal(10) ** -850
+        cre = Decimal(d["nucleus_re"]) + r * Decimal(repr(math.cos(phi)))
+        cim = Decimal(d["nucleus_im"]) + r * Decimal(repr(math.sin(phi)))
+        p, nre, nim, ls = mbx.find_nucleus(format(cre, "f"), format(cim, "f"), "3e-851", 200000, 3600)
+        d["zoom"].update(nucleus_re=nre, nucleus_im=nim, period=p, size_log10=ls)
+        json.dump(d, open(DATA, "w"), indent=1)
+        print("period", p, "size 1e%.2f" % ls)
     if "--regenerate-minibrot" in sys.argv:
         import mbx
 
