@@ -12,6 +12,7 @@ with the repository.
 Usage: python tests/golden/make_truth.py [frame ...]   (default: every frame)
        python tests/golden/make_truth.py --cases [case ...]  (full-frame truth of
        double-path parity cases, truthgen_<case>.npz; default: CASE_TRUTH)
+       python tests/golden/make_truth.py --zoom  (zoom-sequence subsets, truth_zoom.npz)
 """
 import os
 import sys
@@ -93,9 +94,34 @@ def make_case(name):
     print("%s: %d samples in %.0f s, %d interior" % (name, keys.shape[0], time.time() - t, int(np.sum(tn < 0))))
 
 
+# Zoom sequence (zoom.py): for the frames the GPU test renders (240x136), a
+# seeded subset of 48 samples each with its exterior distance (EDE) and escape
+# iteration (truth_zoom.npz: for each frame k, idx_k, N_k, value_k).
+ZOOM_FRAMES = (8, 150, 300, 450, 599)
+ZOOM_W, ZOOM_H = 240, 136
+
+
+def make_zoom():
+    import zoom
+
+    out = {}
+    t = time.time()
+    for k in ZOOM_FRAMES:
+        q = zoom.request(k, ZOOM_W, ZOOM_H)
+        idx = np.sort(np.random.RandomState(700 + k).choice(ZOOM_W * ZOOM_H, size=48, replace=False))
+        keys = np.stack([idx // ZOOM_W, idx % ZOOM_W, np.zeros_like(idx), np.zeros_like(idx)], axis=1)
+        tv, tn = oracle.truth(q.center_re, q.center_im, q.scale, ZOOM_W, ZOOM_H, q.max_iterations, keys, coloring_method=q.coloring_method, bailout=q.bailout,
+                              threads=os.cpu_count(), precision_bits=q.precision_bits)
+        out["idx_%d" % k], out["N_%d" % k], out["value_%d" % k] = idx.astype(np.int32), tn.astype(np.int32), tv.astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "truth_zoom.npz"), **out)
+    print("zoom: %d frames x 48 samples in %.0f s" % (len(ZOOM_FRAMES), time.time() - t))
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
-    if args and args[0] == "--cases":
+    if args and args[0] == "--zoom":
+        make_zoom()
+    elif args and args[0] == "--cases":
         for name in args[1:] or (CASE_TRUTH + DE_CASE_TRUTH):
             make_case(name)
     else:
