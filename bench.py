@@ -415,6 +415,38 @@ def main():
     bat2.close()
     e2e_batch_value = eb_eff / eb_t / 1e9
 
+    # zoom sequence (zoom.py): a stated subset of the 600 frames at the frames'
+    # resolution, EDE, mixed form, one periodic reference orbit shared by every
+    # frame (built once, outside the timed frames); accuracy on the committed
+    # arbitrary-precision subsets of five 240x136 frames of the sequence
+    import zoom
+
+    zsub = list(range(0, zoom.ZOOM_FRAMES, 50)) + [zoom.ZOOM_FRAMES - 1]
+    zbe = mbx.create_compute_backend("cuda", local)
+    zoom.render_sequence(zbe, [zsub[1]], W, H)  # builds the shared orbit
+    zframes = {}
+    z_t0 = time.perf_counter()
+    for k, q, st in zoom.render_sequence(zbe, zsub, W, H):
+        zframes[k] = {"frame_ms": st["total_ms"], "pass_gpu_ms": st["pass_gpu_ms"], "effective_iterations": st["effective_iterations"],
+                      "reused_reference": st["reused_reference"], "reruns": st["fp64_reruns"], "maxiter": q.max_iterations}
+    z_elapsed = time.perf_counter() - z_t0
+    z_acc = {}
+    ztp = os.path.join(ROOT, "tests", "golden", "truth_zoom.npz")
+    if os.path.exists(ztp):
+        zt = np.load(ztp)
+        for k, q, st in zoom.render_sequence(zbe, [8, 150, 300, 450, 599], 240, 136):
+            idx, tn, tv = zt["idx_%d" % k], zt["N_%d" % k], zt["value_%d" % k]
+            ext = (tn > 0) & (q.escape_iteration[idx] == tn)
+            z_acc[k] = {"escape_iteration_identical": float(np.mean(q.escape_iteration[idx] == tn)),
+                        "max_rel_dDE": float(np.max(np.abs(q.iterations[idx][ext].astype(np.float64) - tv[ext]) / np.abs(tv[ext]), initial=0.0))}
+    zbe.close()
+    zoom_line = {"frames": len(zsub), "subset": "frames 0, 50, ..., 550, 599 of 600 (half-width 10^(-1000 k/599), maxiter 1e3 -> 5e6 geometric, EDE)",
+                 "ms_total": z_elapsed * 1e3, "frame_ms": {str(k): v["frame_ms"] for k, v in zframes.items()},
+                 "gpixel_iter_per_s": sum(v["effective_iterations"] for v in zframes.values()) / z_elapsed / 1e9, "unit": UNIT,
+                 "shared_orbit": "period-%d nucleus, built once; reused by %d of %d frames (the shallow ones, half-width >= 2e-6, use no reference)"
+                                 % (zoom.target()[2], sum(v["reused_reference"] for v in zframes.values()), len(zsub)),
+                 "accuracy_vs_truth_240x136": z_acc}
+
     # plain FP64 GPU form on a sample of the same views, and accuracy vs it
     if args.plain_sample == "full":
         pw, ph = W, H
@@ -502,6 +534,7 @@ def main():
                 "autotuned": tuning,
                 "batched": batched,
                 "image_epilogue": epilogue,
+                "zoom_sequence": zoom_line,
                 "reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_batch_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": eb_t / 2 * 1e3,

@@ -163,13 +163,17 @@ int mbx_find_nucleus(const char* center_re, const char* center_im, const char* r
 /* Batched rendering of n (1..256) frames (no reference counterpart: the
  * reference renders one frame per compute() call). Each frame is prepared as
  * by mbx_compute (reference orbit, BLA tables, outputs); the probe and main
- * passes of every frame in the mixed form (floatexp, no DE colouring, sub 1)
- * then run in shared persistent launches — one batch-wide work counter over
- * all frames' samples, then the double-float and FP64 rerun tiers — captured
- * once as a CUDA graph and replayed while the batch keeps its shape. Other
- * frames are rendered one by one. Results are identical to mbx_compute of
- * each frame. view_stats (n entries) and batch_stats may be NULL; the shared
- * passes' counters go to batch_stats. Frames need fewer than 65536 sample rows. */
+ * passes of every perturbation frame in the mixed form (any colouring) then
+ * run in shared persistent launches — one batch-wide work counter over all
+ * frames' samples, then the double-float tier — captured once as a CUDA graph
+ * and replayed while the batch keeps its shape; what no lane tier vouches for
+ * is finished per frame in the exact form, and the adaptive-supersampling
+ * passes of supersampled frames run per frame after the graph, on the frames'
+ * own streams from concurrent host threads. Other frames (shallow, exact
+ * form, and supersampled frames while the learned ordering is on) are rendered
+ * one by one. Results are identical to mbx_compute of each frame. view_stats
+ * (n entries) and batch_stats may be NULL; the shared passes' counters go to
+ * batch_stats. Frames need fewer than 65536 sample rows. */
 int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats);
 
 /* Learned ordering of the batched main pass (no reference counterpart). With

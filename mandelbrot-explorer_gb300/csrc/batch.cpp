@@ -409,6 +409,36 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
                 }
             }
         }
+        {
+            // supersampled frames: each engine's adaptive-supersampling passes on
+            // its own stream, driven from concurrent host threads so that the
+            // frames' passes overlap on the device
+            std::vector<unsigned> vint((size_t)nv, 0u);
+            cudaMemcpyAsync(vint.data(), d_view_interior_, sizeof(unsigned) * nv, cudaMemcpyDeviceToHost, st_);
+            bs.d2h_bytes += (long long)(sizeof(unsigned) * nv);
+            e = cudaStreamSynchronize(st_);
+            if (e != cudaSuccess) return cuda_fail(err, "interior gate readback", e);
+            std::vector<int> ss;
+            for (int k = 0; k < nv; ++k)
+                if (reqs[deferred[k]].sub > 1) ss.push_back(k);
+            if (!ss.empty()) {
+                const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+                const int lanes = std::max(1, std::min({(int)ss.size(), 8, (int)hw}));
+                std::vector<int> rcs(ss.size(), MBX_OK);
+                auto work = [&](int t) {
+                    for (size_t q = (size_t)t; q < ss.size(); q += (size_t)lanes) rcs[q] = eng_[deferred[ss[q]]]->batch_supersample(vint[(size_t)ss[q]] > 0);
+                };
+                std::vector<std::thread> th;
+                for (int t = 1; t < lanes; ++t) th.emplace_back(work, t);
+                work(0);
+                for (auto& x : th) x.join();
+                for (size_t q = 0; q < ss.size(); ++q)
+                    if (rcs[q] != MBX_OK) {
+                        err = eng_[deferred[ss[q]]]->error();
+                        return rcs[q];
+                    }
+            }
+        }
         for (int k = 0; k < nv; ++k) {
             const int i = deferred[k];
             rc = eng_[i]->batch_finish(reqs[i], &vst[i]);

@@ -1950,6 +1950,18 @@ int Engine::batch_exact_rerun(std::vector<uint64_t>& keys, bool interior_seen) {
     return MBX_OK;
 }
 
+// The adaptive supersampling of a batched frame (mp.cpp:1789-2006), after the
+// batch's shared passes gave it its centre samples; interior detection as the
+// frame's probe left it.
+int Engine::batch_supersample(bool interior_seen) {
+    if (!(SUB_ > 1 && (cm_ & 1))) return MBX_OK;
+    const bool interior = use_interior_;
+    if (!interior_seen) use_interior_ = false;
+    const int rc = supersample(batch_ref_it_);
+    use_interior_ = interior;
+    return rc;
+}
+
 int Engine::batch_finish(const mbx_request& r, mbx_stats* out_stats) {
     const size_t nsamp = (size_t)r.width * r.height * r.sub * r.sub;
     const double t0 = now_ms();
@@ -2155,7 +2167,9 @@ int Engine::render(mpf_ptr c_re, mpf_ptr c_im, mpf_ptr scale, int full_h, int ro
     rc = flush_ref_value();
     if (rc != MBX_OK) return rc;
     if (progress) *progress = 0.08f;
-    if (batch_slot_ && use_floatexp_ && mixed_active() && SUB_ == 1) {
+    // (the learned ordering's per-sample costs assume sub 1: with it on,
+    // supersampled frames render on their own)
+    if (batch_slot_ && use_floatexp_ && mixed_active() && (SUB_ == 1 || !batch_slot_->want_cost)) {
         batch_ref_it_ = ref_it;
         fill_batch_slot(); // the probe and main passes run in the batch's launches
         return MBX_OK;

@@ -92,6 +92,7 @@ class Engine {
     // frame when it is not eligible (mixed form, floatexp, no DE, sub 1);
     // finish copies host outputs and completes the stats of a deferred frame.
     int compute_deferred(const mbx_request& r, BatchSlot* slot, mbx_stats* st);
+    int batch_supersample(bool interior_seen);
     int batch_finish(const mbx_request& r, mbx_stats* st);
     // the exact form over a deferred frame's samples the batched tiers could
     // not vouch for (keys as key_pack; emptied on success); interior_seen: the

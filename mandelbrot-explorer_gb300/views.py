@@ -107,6 +107,44 @@ def minibrot_view(seed: int = 1000, width: int = 1920, height: int = 1080, max_i
     }
 
 
+# The batching workload: 64 seed-drawn views of uneven shape — square sizes
+# uniform over {256, 512, 1024, 2048, 4096}, log10 half-width uniform in
+# [-600, -20], maxiter log-uniform in [1e4, 1e6], 3x3 adaptive supersampling
+# (sub 3 with MBX_SUPER_SAMPLING) on a seed-drawn half of them — centred a
+# seed-drawn vector of 0.3 half-widths from the zoom target nucleus (period
+# 72852) so that every view holds structure. size_div divides the sizes (a
+# stated sample of the workload).
+def c3_views(seed: int = 3, n: int = 64, size_div: int = 1):
+    d = nucleus()["zoom"]
+    rng = np.random.RandomState(seed)
+    ss = set(rng.permutation(n)[: n // 2].tolist())
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    out = []
+    for i in range(n):
+        size = int(rng.choice([256, 512, 1024, 2048, 4096])) // size_div
+        lhw = float(rng.uniform(20.0, 600.0))
+        maxiter = int(round(10 ** rng.uniform(4.0, 6.0)))
+        ang = rng.uniform(0.0, 2.0 * math.pi)
+        hw = Decimal(10) ** Decimal(repr(-lhw))
+        cre = Decimal(d["nucleus_re"]) + Decimal("0.3") * hw * Decimal(repr(math.cos(ang)))
+        cim = Decimal(d["nucleus_im"]) + Decimal("0.3") * hw * Decimal(repr(math.sin(ang)))
+        scale = Decimal(2) / hw
+        out.append({
+            "center_re": format(cre, "f"),
+            "center_im": format(cim, "f"),
+            "scale": format(scale.normalize(), "E").replace("E+", "e"),
+            "width": size,
+            "height": size,
+            "sub": 3 if i in ss else 1,
+            "coloring_method": 1 if i in ss else 0,
+            "max_iterations": maxiter,
+            "bailout": 256.0,
+            "label": "c3-%02d" % i,
+            "precision_bits": int(lhw * math.log2(10)) + 128,
+        })
+    return out
+
+
 # Frames with committed arbitrary-precision truth subsets (tests/golden/make_truth.py).
 TRUTH_FRAMES = ("1e-300", "1e-1000", "1e-1000-minibrot")
 
