@@ -447,6 +447,31 @@ def main():
                                  % (zoom.target()[2], sum(v["reused_reference"] for v in zframes.values()), len(zsub)),
                  "accuracy_vs_truth_240x136": z_acc}
 
+    # batching workload (views.c3_views): all 64 views at 1/8 of their linear
+    # sizes (32..512 square, half of them 3x3 adaptive supersampling), one
+    # mbx_compute_batch call per step with the references resident: the views'
+    # probe and main passes in one CUDA graph, then the supersampling passes
+    c3 = views.c3_views(size_div=8)
+    c3be = mbx.create_compute_backend("cuda", local)
+
+    def c3_reqs():
+        return [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], v["width"], v["height"], v["max_iterations"], sub=v["sub"],
+                                   coloring_method=v["coloring_method"], bailout=v["bailout"], precision_bits=v["precision_bits"],
+                                   precision_mode=mbx.PRECISION_MIXED, reuse_reference=True) for v in c3]
+    for _ in range(2):
+        assert c3be.compute_batch(c3_reqs()) == mbx.OK, c3be.last_error()
+    c3_t, c3_eff, c3_gpu = 0.0, 0, 0.0
+    for _ in range(args.steps):
+        rq = c3_reqs()
+        t = time.perf_counter()
+        assert c3be.compute_batch(rq) == mbx.OK, c3be.last_error()
+        c3_t += time.perf_counter() - t
+        c3_eff += c3be.last_batch_stats.effective_iterations + sum(s_.effective_iterations for s_ in c3be.last_view_stats)
+        c3_gpu += c3be.last_batch_stats.pass_gpu_ms
+    c3be.close()
+    c3_line = {"views": len(c3), "sample": "all 64 seed-drawn views at 1/8 of their linear sizes (32..512 square; 32 with 3x3 adaptive supersampling), references resident",
+               "ms_per_batch": c3_t / args.steps * 1e3, "shared_graph_gpu_ms": c3_gpu / args.steps, "gpixel_iter_per_s": c3_eff / c3_t / 1e9, "unit": UNIT}
+
     # plain FP64 GPU form on a sample of the same views, and accuracy vs it
     if args.plain_sample == "full":
         pw, ph = W, H
@@ -535,6 +560,7 @@ def main():
                 "batched": batched,
                 "image_epilogue": epilogue,
                 "zoom_sequence": zoom_line,
+                "batch_c3": c3_line,
                 "reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_batch_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": eb_t / 2 * 1e3,
