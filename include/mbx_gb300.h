@@ -96,14 +96,17 @@ typedef struct {
     int reused_reference;           /* 1 when the cached reference was reused */
     long long rebases;              /* rebases taken (mixed form) */
     long long fp64_reruns;          /* mixed form: samples rerun in double-float (FP32 error estimate too large) */
-    double rerun_gpu_ms;            /* device time of the reruns (included in pass_gpu_ms) */
+    double rerun_gpu_ms;            /* device time of the reruns (included in pass_gpu_ms); batch: the main
+                                       pass's double-float tier with its queue's compaction (and training, mode 1) */
     long long fp64_reruns_fp64;     /* of those, samples rerun again in FP64: the exact form (double-float estimate too large) */
-    double rerun_fp64_gpu_ms;       /* device time of the exact-form reruns (included in rerun_gpu_ms) */
+    double rerun_fp64_gpu_ms;       /* device time of the exact-form reruns (included in rerun_gpu_ms); batch:
+                                       host wall time of the views' concurrent exact-form leftovers (after pass_gpu_ms) */
     long long exact_steps;          /* mixed form: steps taken in floatexp (orbit or delta below the lane type's range) */
     long long fe_rebases;           /* mixed form: rebases decided in floatexp (inside the margin, end of reference) */
     long long exact_reruns;         /* mixed form: samples finished by the exact form (no tier could vouch for them; equals fp64_reruns_fp64) */
     long long h2d_bytes, d2h_bytes; /* bytes copied host->device / device->host by the call (counted at each copy) */
-    double fp32_pass_gpu_ms;        /* mixed form: CUDA-event time of the FP32 lane passes alone (probe and main) */
+    double fp32_pass_gpu_ms;        /* mixed form: CUDA-event time of the FP32 lane passes alone (probe and main;
+                                       batch: the main pass) */
     long long fp32_pass_steps;      /* mixed form: delta steps executed by those passes */
     long long fp32_pass_bla_applies;/* mixed form: BLA skips taken by those passes */
     long long fp32_unvouched_interior; /* mixed form: of fp64_reruns, interior decisions the FP32 estimate could not vouch for */
@@ -176,19 +179,23 @@ int mbx_find_nucleus(const char* center_re, const char* center_im, const char* r
  * batch_stats. Frames need fewer than 65536 sample rows. */
 int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats);
 
-/* Learned ordering of the batched main pass (no reference counterpart). With
- * mode 1, each batch's main-pass samples start in decreasing cost as predicted
- * by a BF16 MLP (24 -> 64 -> 64 -> 1) from the probe pass's costs around them;
- * after the pass the model trains on the batch's measured per-sample costs
- * (tensor-core kernels, Adam), so the next batch uses it. Mode 2 orders with
- * the model as it stands (no training). An untrained model keeps the natural
- * order. Outputs are identical in every mode. 0 (default): natural order. */
+/* Learned ordering of the batched main pass (no reference counterpart). A
+ * BF16 MLP (24 -> 64 -> 64 -> 1) predicts each 16x16 tile's mean FP32-lane
+ * cost from the probe pass (its four probe cells' costs, BLA-skip fractions
+ * and mean skip lengths, interior flags, the neighbouring tiles' costs, view
+ * features). With mode 1 the main FP32 pass takes the views in decreasing
+ * predicted cost and each view's samples in decreasing predicted tile cost;
+ * after the passes the model trains on the batch's tiles and their measured
+ * costs (tcgen05 kernels, Adam, 32 steps), so the next batch uses it. Mode 2
+ * orders with the model as it stands (no training). A fresh context's model
+ * predicts a tile's mean probe cost. Outputs are identical in every mode.
+ * 0 (default): natural order. */
 int mbx_set_batch_scheduling(mbx_context* ctx, int mode);
 
 /* Diagnostics of the ordering model: parameters (5825 floats: W1 [64][24], b1
  * [64], W2 [64][64], b2 [64], w3 [64], b3) set and/or read, and the gradients
- * of one training step (mean squared error / 2 over the first 128 of n >= 128
- * samples: features n x 24, targets n) without an update. */
+ * of one training step over n >= 128 samples (mean squared error / 2;
+ * features n x 24, targets n) without an update. */
 int mbx_schedule_params(mbx_context* ctx, const float* set, float* get);
 int mbx_schedule_gradient(mbx_context* ctx, const float* features, const float* targets, int n, float* grad);
 

@@ -6,6 +6,7 @@
 //   gate -> main: FP32, double-float, FP64 lane passes -> counters to the host.
 #include "batch.h"
 
+#include <chrono>
 #include <thread>
 
 #include <algorithm>
@@ -24,14 +25,17 @@ BatchRunner::~BatchRunner() {
     if (st_) cudaStreamSynchronize(st_);
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
-    for (void* p : {(void*)d_probe_, (void*)d_main_, (void*)d_ctr_, (void*)d_view_interior_, (void*)d_qa_, (void*)d_qb_, (void*)d_qo_, (void*)d_main_total_,
+    for (void* p : {(void*)d_probe_, (void*)d_main_, (void*)d_ctr_, (void*)d_view_interior_, (void*)d_qa_, (void*)d_qb_, (void*)d_qo_, (void*)d_main_total_, (void*)d_flag_, (void*)d_fsum_,
                     (void*)sched_.params, (void*)sched_.adam_m, (void*)sched_.adam_v, (void*)sched_.ready, (void*)sched_.steps, (void*)sched_.loss,
-                    (void*)sched_.hist, (void*)sched_.cursor, (void*)sched_.bucket, (void*)sched_.X, (void*)sched_.T})
+                    (void*)sched_.hist, (void*)sched_.bucket, (void*)sched_.tile_bucket, (void*)sched_.X, (void*)sched_.T, (void*)sched_.grad,
+                    (void*)sched_.err})
         if (p) cudaFree(p);
     if (h_desc_) cudaFreeHost(h_desc_);
     if (h_ctr_) cudaFreeHost(h_ctr_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    for (cudaEvent_t ev : evm_)
+        if (ev) cudaEventDestroy(ev);
     if (st_) cudaStreamDestroy(st_);
 }
 
@@ -45,7 +49,8 @@ void BatchRunner::reset_cancel() {
 int BatchRunner::ensure_engines(int n, std::string& err) {
     if (!st_) {
         if (cudaSetDevice(device_) != cudaSuccess || cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess) {
+            cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess || cudaEventCreate(&evm_[0]) != cudaSuccess ||
+            cudaEventCreate(&evm_[1]) != cudaSuccess) {
             err = "batch stream creation failed";
             return MBX_E_CUDA;
         }
@@ -62,7 +67,18 @@ int BatchRunner::ensure_engines(int n, std::string& err) {
     return MBX_OK;
 }
 
-int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err) {
+int BatchRunner::ensure_buffers(int nviews, unsigned capacity, unsigned tiles, std::string& err) {
+    if (tiles > cap_tiles_) {
+        if (sched_.tile_bucket) cudaFree(sched_.tile_bucket);
+        sched_.tile_bucket = nullptr;
+        if (cudaMalloc(&sched_.tile_bucket, tiles) != cudaSuccess) {
+            err = "batch tile buffer allocation failed";
+            cap_tiles_ = 0;
+            return MBX_E_NOMEM;
+        }
+        cap_tiles_ = tiles;
+        g_views_ = -1;
+    }
     if (nviews > cap_views_) {
         if (d_probe_) cudaFree(d_probe_);
         if (d_main_) cudaFree(d_main_);
@@ -93,12 +109,14 @@ int BatchRunner::ensure_buffers(int nviews, unsigned capacity, std::string& err)
             *q = nullptr;
         }
         if (sched_.bucket) cudaFree(sched_.bucket);
-        if (sched_.hist) cudaFree(sched_.hist);
+        if (d_flag_) cudaFree(d_flag_);
+        if (d_fsum_) cudaFree(d_fsum_);
         sched_.bucket = nullptr;
-        sched_.hist = nullptr;
+        d_flag_ = nullptr;
+        d_fsum_ = nullptr;
         if (cudaMalloc(&d_qa_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&d_qb_, sizeof(uint64_t) * capacity) != cudaSuccess ||
-            cudaMalloc(&d_qo_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&sched_.bucket, capacity + 8 * 1024) != cudaSuccess ||
-            cudaMalloc(&sched_.hist, sizeof(unsigned) * 32 * ((capacity + 8 * 1024 - 1) / 1024 + 8)) != cudaSuccess) {
+            cudaMalloc(&d_qo_, sizeof(uint64_t) * capacity) != cudaSuccess || cudaMalloc(&sched_.bucket, sizeof(uint16_t) * capacity) != cudaSuccess ||
+            cudaMalloc(&d_flag_, capacity) != cudaSuccess || cudaMalloc(&d_fsum_, sizeof(unsigned) * (flag_blocks(capacity) + 1)) != cudaSuccess) {
             err = "batch queue allocation failed";
             cap_samples_ = 0;
             return MBX_E_NOMEM;
@@ -123,9 +141,10 @@ int BatchRunner::ensure_sched(std::string& err) {
     if (cudaMalloc(&sched_.params, sizeof(float) * N) != cudaSuccess || cudaMalloc(&sched_.adam_m, sizeof(float) * N) != cudaSuccess ||
         cudaMalloc(&sched_.adam_v, sizeof(float) * N) != cudaSuccess || cudaMalloc(&sched_.ready, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&sched_.steps, sizeof(int)) != cudaSuccess || cudaMalloc(&sched_.loss, sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&sched_.cursor, sizeof(unsigned) * 32) != cudaSuccess ||
-        cudaMalloc(&sched_.X, sizeof(__nv_bfloat16) * kSchedSamples * kSchedFeatures) != cudaSuccess ||
-        cudaMalloc(&sched_.T, sizeof(float) * kSchedSamples) != cudaSuccess) {
+        cudaMalloc(&sched_.grad, sizeof(float) * N) != cudaSuccess || cudaMalloc(&sched_.err, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&sched_.hist, sizeof(unsigned) * sched_scratch_words()) != cudaSuccess ||
+        cudaMalloc(&sched_.X, sizeof(__nv_bfloat16) * kSchedTiles * kSchedFeatures) != cudaSuccess ||
+        cudaMalloc(&sched_.T, sizeof(float) * kSchedTiles) != cudaSuccess) {
         err = "scheduler allocation failed";
         return MBX_E_NOMEM;
     }
@@ -201,8 +220,10 @@ int BatchRunner::schedule_gradient(const float* features, const float* targets, 
     return e == cudaSuccess ? MBX_OK : cuda_fail(err, "gradient check", e);
 }
 
-int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, int deriv, std::string& err) {
-    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_cancel_ == cancel_flag && g_schedule_ == schedule_ && g_deriv_ == deriv) return MBX_OK;
+int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_total, unsigned tile_total, volatile int* cancel_flag, int deriv, std::string& err) {
+    if (exec_ && g_views_ == nviews && g_probe_ == probe_total && g_main_ == main_total && g_tiles_ == tile_total && g_cancel_ == cancel_flag &&
+        g_schedule_ == schedule_ && g_deriv_ == deriv)
+        return MBX_OK;
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     exec_ = nullptr;
@@ -223,17 +244,28 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
         a.view_interior = vint;
         a.cancel = cancel_flag;
         a.deriv = deriv;
-        // FP32 over all samples (in the learned order when given)
+        // FP32 over all samples (in the learned order when given); the main
+        // pass flags its leftovers per sample
         a.total = total;
-        a.queue = order;
-        a.queue_n = order ? d_main_total_ : nullptr;
+        a.order = order;
         a.ctr = d_ctr_ + c0;
         a.next_queue = d_qa_;
+        if (!probe_only) {
+            a.rerun_flag = d_flag_;
+            cudaMemsetAsync(d_flag_, 0, total, st_);
+            // event-record nodes of the graph (plain records in a capture add none)
+            cudaEventRecordWithFlags(evm_[0], st_, cudaEventRecordExternal);
+        }
         launch_batch_pass(0, a, nsm, st_);
         if (probe_only) return;
-        // double-float over the FP32 pass's queue; what it cannot vouch for
-        // is queued for the views' exact form (host side, after the graph)
-        a.queue = d_qa_;
+        cudaEventRecordWithFlags(evm_[1], st_, cudaEventRecordExternal);
+        // double-float over the leftovers in the natural order (the FP32 pass
+        // is done with d_qo_); what it cannot vouch for is queued for the
+        // views' exact form (host side, after the graph)
+        launch_flag_compact(views, nviews, total, d_flag_, d_fsum_, d_qo_, st_);
+        a.order = nullptr;
+        a.rerun_flag = nullptr;
+        a.queue = d_qo_;
         a.queue_n = &d_ctr_[c0].rerun_n;
         a.ctr = d_ctr_ + c0 + 1;
         a.next_queue = d_qb_;
@@ -243,9 +275,9 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     launch_batch_gate(d_main_, nviews, d_view_interior_, st_);
     if (schedule_) {
         sched_probe_grid(d_probe_, d_main_, nviews, probe_total, st_);
-        sched_order(sched_, d_main_, nviews, main_total, nsm, d_qo_, st_);
+        sched_order(sched_, d_main_, nviews, main_total, tile_total, nsm, d_qo_, st_);
         tiers(d_main_, main_total, 2, nullptr, d_qo_, false);
-        if (schedule_ == 1) sched_train(sched_, d_main_, nviews, main_total, kSchedTrainSteps, 2e-3f, st_);
+        if (schedule_ == 1) sched_train(sched_, d_main_, nviews, tile_total, kSchedTrainSteps, 2e-3f, st_);
     } else {
         tiers(d_main_, main_total, 2, nullptr, nullptr, false);
     }
@@ -257,6 +289,7 @@ int BatchRunner::build_graph(int nviews, unsigned probe_total, unsigned main_tot
     g_views_ = nviews;
     g_probe_ = probe_total;
     g_main_ = main_total;
+    g_tiles_ = tile_total;
     g_cancel_ = cancel_flag;
     g_schedule_ = schedule_;
     g_deriv_ = deriv;
@@ -300,7 +333,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
     mbx_stats bs = mbx_stats();
     if (!deferred.empty()) {
         const int nv = (int)deferred.size();
-        unsigned probe_total = 0, main_total = 0;
+        unsigned probe_total = 0, main_total = 0, tile_total = 0;
         for (int k = 0; k < nv; ++k) {
             const int i = deferred[k];
             if (reqs[i].height * reqs[i].sub >= (1 << 16)) {
@@ -309,10 +342,12 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             }
             slots[i].probe.base = probe_total;
             slots[i].main.base = main_total;
+            slots[i].probe.tile_base = slots[i].main.tile_base = tile_total;
             probe_total += slots[i].probe.count;
             main_total += slots[i].main.count;
+            tile_total += (unsigned)(slots[i].main.tw * slots[i].main.th);
         }
-        rc = ensure_buffers(nv, std::max(probe_total, main_total), err);
+        rc = ensure_buffers(nv, std::max(probe_total, main_total), tile_total, err);
         if (rc != MBX_OK) return rc;
         for (int k = 0; k < nv; ++k) {
             h_desc_[k] = slots[deferred[k]].probe;
@@ -336,7 +371,7 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
         bs.h2d_bytes += (long long)(sizeof(unsigned) + 2 * sizeof(ViewDesc) * nv);
         int deriv = 0;
         for (int k = 0; k < nv; ++k) deriv |= h_desc_[nv + k].p.g.deriv ? 1 : 0;
-        rc = build_graph(nv, probe_total, main_total, cancel_flag, deriv, err);
+        rc = build_graph(nv, probe_total, main_total, tile_total, cancel_flag, deriv, err);
         if (rc != MBX_OK) return rc;
         cudaEventRecord(ev0_, st_);
         cudaError_t e = cudaGraphLaunch(exec_, st_);
@@ -350,9 +385,28 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
             err = "cancelled";
             return MBX_E_CANCELLED;
         }
+        if (schedule_) {
+            int terr = 0;
+            e = cudaMemcpy(&terr, sched_.err, sizeof(int), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return cuda_fail(err, "scheduler status", e);
+            if (terr) {
+                err = "ordering model: a tensor-core completion wait ran out of its limit";
+                return MBX_E_CUDA;
+            }
+        }
         bs.pass_gpu_ms = ms;
+        // the main FP32 pass alone; the rest of the graph's main part is the
+        // regrouping and the double-float tier
+        float f32 = 0.0f, rest = 0.0f;
+        if (cudaEventElapsedTime(&f32, evm_[0], evm_[1]) == cudaSuccess && cudaEventElapsedTime(&rest, evm_[1], ev1_) == cudaSuccess) {
+            bs.fp32_pass_gpu_ms = f32;
+            bs.rerun_gpu_ms = rest;
+        } else {
+            (void)cudaGetLastError(); // no split: leave no error behind for later calls
+        }
         bs.d2h_bytes += (long long)(4 * sizeof(Counters)); // the graph's counter readback
-        bs.kernel_launches = 5; // probe FP32; gate; main FP32, double-float (two widths)
+        // probe FP32; gate; main FP32; regrouping (3); double-float (two widths); ordering and training
+        bs.kernel_launches = 8 + (schedule_ ? 6 + (schedule_ == 1 ? sched_train_launches(kSchedTrainSteps) : 0) : 0);
         bs.passes = 2;
         for (int c = 0; c < 4; ++c) {
             const Counters& k = h_ctr_[c];
@@ -401,13 +455,32 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
                 }
                 per[(size_t)v].push_back(k & ((1ull << kBatchViewShift) - 1ull));
             }
-            for (int k = 0; k < nv; ++k) {
-                rc = eng_[deferred[k]]->batch_exact_rerun(per[(size_t)k], vint[(size_t)k] > 0);
-                if (rc != MBX_OK) {
-                    err = eng_[deferred[k]]->error();
-                    return rc;
+            // each view's leftovers are a few long FP64 dependency chains: the
+            // engines run them on their own streams from concurrent host
+            // threads, so the views' chains overlap on the device
+            std::vector<int> ex;
+            for (int k = 0; k < nv; ++k)
+                if (!per[(size_t)k].empty()) ex.push_back(k);
+            const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+            const int lanes = std::max(1, std::min({(int)ex.size(), 16, (int)hw}));
+            std::vector<int> rcs(ex.size(), MBX_OK);
+            auto work = [&](int t) {
+                for (size_t q = (size_t)t; q < ex.size(); q += (size_t)lanes) {
+                    const int k = ex[q];
+                    rcs[q] = eng_[deferred[k]]->batch_exact_rerun(per[(size_t)k], vint[(size_t)k] > 0);
                 }
-            }
+            };
+            const auto t0 = std::chrono::steady_clock::now();
+            std::vector<std::thread> th;
+            for (int t = 1; t < lanes; ++t) th.emplace_back(work, t);
+            work(0);
+            for (auto& x : th) x.join();
+            bs.rerun_fp64_gpu_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            for (size_t q = 0; q < ex.size(); ++q)
+                if (rcs[q] != MBX_OK) {
+                    err = eng_[deferred[ex[q]]]->error();
+                    return rcs[q];
+                }
         }
         {
             // supersampled frames: each engine's adaptive-supersampling passes on

@@ -30,13 +30,14 @@ class BatchRunner {
 
   private:
     int ensure_engines(int n, std::string& err);
-    int ensure_buffers(int nviews, unsigned capacity, std::string& err);
-    int build_graph(int nviews, unsigned probe_total, unsigned main_total, volatile int* cancel_flag, int deriv, std::string& err);
+    int ensure_buffers(int nviews, unsigned capacity, unsigned tiles, std::string& err);
+    int build_graph(int nviews, unsigned probe_total, unsigned main_total, unsigned tile_total, volatile int* cancel_flag, int deriv, std::string& err);
 
     int device_;
     std::vector<std::unique_ptr<Engine>> eng_;
     cudaStream_t st_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t evm_[2] = {nullptr, nullptr}; // in the graph: main FP32 pass start and end
     ViewDesc* d_probe_ = nullptr;
     ViewDesc* d_main_ = nullptr;
     ViewDesc* h_desc_ = nullptr;   // pinned staging: probe descriptors then main descriptors
@@ -50,7 +51,8 @@ class BatchRunner {
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int g_views_ = -1;
-    unsigned g_probe_ = 0, g_main_ = 0;
+    unsigned g_probe_ = 0, g_main_ = 0, g_tiles_ = 0;
+    unsigned cap_tiles_ = 0;
     volatile int* g_cancel_ = nullptr;
     int g_schedule_ = -1;
     int g_deriv_ = -1;     // the captured graph's lanes carry the derivative (DE colourings)
@@ -58,7 +60,9 @@ class BatchRunner {
     int schedule_ = 0;
     SchedState sched_{};
     bool sched_ready_ = false;
-    uint64_t* d_qo_ = nullptr;       // ordered main-pass queue
+    uint64_t* d_qo_ = nullptr;       // the main FP32 pass's order (sample indices), then the double-float queue
+    uint8_t* d_flag_ = nullptr;      // main FP32 pass: per sample, left to the double-float tier
+    unsigned* d_fsum_ = nullptr;     // block sums of the flags' compaction
     unsigned* d_main_total_ = nullptr;
     unsigned h_main_total_ = 0;
     int ensure_sched(std::string& err);

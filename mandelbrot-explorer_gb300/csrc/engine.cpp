@@ -275,7 +275,7 @@ void Engine::release_device() {
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
                     (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZq_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dblamax_.p,
                     (void*)drerun_keys_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p,
-                    (void*)dcost_.p, (void*)dpgrid_.p, (void*)ddpxy_.p, (void*)ddpxyf_.p})
+                    (void*)dcost_.p, (void*)dblac_.p, (void*)dpgrid_.p, (void*)ddpxy_.p, (void*)ddpxyf_.p})
         if (p) cudaFree(p);
     if (dctr_) cudaFree(dctr_);
     if (ev0_) cudaEventDestroy(ev0_);
@@ -1906,11 +1906,16 @@ void Engine::fill_batch_slot() {
     mn.interior_gate = 1;
     mn.count = (unsigned)mn.f.px.n;
     pr.f.out.cost = mn.f.out.cost = nullptr;
+    pr.f.out.bla = mn.f.out.bla = nullptr;
     pr.pgrid = mn.pgrid = nullptr;
     pr.pgw = mn.pgw = (W_ + 7) / 8;
     pr.pgh = mn.pgh = (H_ + 7) / 8;
-    if (batch_slot_->want_cost && ensure(dcost_, (size_t)W_ * H_) && ensure(dpgrid_, (size_t)mn.pgw * mn.pgh)) {
+    pr.tw = mn.tw = (W_ + 15) / 16;
+    pr.th = mn.th = (H_ + 15) / 16;
+    pr.tile_base = mn.tile_base = 0; // set by the batch
+    if (batch_slot_->want_cost && ensure(dcost_, (size_t)W_ * H_) && ensure(dblac_, (size_t)W_ * H_) && ensure(dpgrid_, (size_t)mn.pgw * mn.pgh)) {
         pr.f.out.cost = mn.f.out.cost = dcost_.p;
+        pr.f.out.bla = mn.f.out.bla = dblac_.p;
         pr.pgrid = mn.pgrid = dpgrid_.p;
     }
     batch_slot_->probe = pr;

@@ -229,8 +229,9 @@ class Engine {
     bool blamax_ok_ = false; // dblamax_ holds the current reference's table
     DevBuf<BlaDF> dbladf_;
     DevBuf<df2> dZdf_;
-    DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample lane cost
-    DevBuf<float2> dpgrid_;   // and the probe pass's cost per 8x8 cell
+    DevBuf<uint32_t> dcost_;  // batch learned ordering: per-sample FP32-lane cost
+    DevBuf<uint32_t> dblac_;  // its BLA skips
+    DevBuf<float4> dpgrid_;   // and the probe pass's record per 8x8 cell
     DevBuf<double> ddpxy_;    // mixed passes: sample offsets per column then per row
     DevBuf<float> ddpxyf_;    // (their float roundings)
     std::vector<double> hdpxy_;

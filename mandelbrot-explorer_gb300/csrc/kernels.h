@@ -113,6 +113,7 @@ struct Outputs {
     uint8_t* done;   // per list entry: 1 finished, 0 pending
     uint8_t* gmp;    // per list entry: needs the arbitrary-precision recompute
     uint32_t* cost = nullptr; // lane passes: per sample (getIndex layout, sub 1) lane steps + 4 per BLA skip
+    uint32_t* bla = nullptr;  // with cost: BLA skips of the sample's FP32 lane (learned ordering's probe features)
 };
 
 struct Counters {
@@ -263,8 +264,11 @@ struct ViewDesc {
     unsigned base;           // first batch-wide sample index of this view
     unsigned count;          // samples of this view in the pass
     int interior_gate;       // main pass: interior detection follows the probe's interior count
-    float2* pgrid;           // learned ordering: probe-pass cost and interior flag per 8x8 cell
+    float4* pgrid;           // learned ordering, per 8x8 cell of the probe: log2(1 + cost) / 24, interior,
+                             // fraction of iterations BLA skipped, log2(1 + mean skip length) / 24
     int pgw, pgh;
+    unsigned tile_base;      // first batch-wide 16x16 tile of this view
+    int tw, th;              // its tiles across and down
 };
 
 // Batch-wide pass arguments. Queue entries are sample keys with the view index
@@ -275,6 +279,8 @@ struct BatchArgs {
     unsigned total;          // sample count (FP32 pass)
     const uint64_t* queue;   // rerun passes: queue of keys; null for the FP32 pass
     const unsigned* queue_n; // its length (on the device)
+    const uint64_t* order;   // FP32 pass: the batch-wide sample indices in the order to take them (null: natural)
+    uint8_t* rerun_flag;     // FP32 pass: per batch-wide sample, set when it is left to the next tier (null: queue it)
     unsigned capacity;       // queue capacity
     Counters* ctr;           // work counter and totals of this pass
     uint64_t* next_queue;    // where samples this pass cannot vouch for go (null: none)
@@ -293,5 +299,9 @@ constexpr int kBatchViewShift = 56;
 constexpr int kBatchMaxViews = 256;
 cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_t st); // tier 0 FP32, 1 double-float, 2 FP64
 cudaError_t launch_batch_gate(ViewDesc* views, int n, const unsigned* view_interior, cudaStream_t st);
+// the rerun queue of the flagged samples, in the batch's natural order (view
+// by view, rows of samples): sums holds flag_blocks(total) words
+unsigned flag_blocks(unsigned total);
+cudaError_t launch_flag_compact(const ViewDesc* views, int nv, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st);
 
 } // namespace mbx

@@ -456,7 +456,8 @@ class CudaComputeBackend:
         return out
 
     def schedule_gradient(self, features, targets) -> np.ndarray:
-        """Gradients of one training step of the ordering model (no update)."""
+        """Gradients of one training step of the ordering model over all rows
+        of features (n x 24, n >= 128) and targets (n), without an update."""
         x = np.ascontiguousarray(features, dtype=np.float32)
         t = np.ascontiguousarray(targets, dtype=np.float32)
         g = np.empty(SCHED_PARAMS, np.float32)

@@ -43,7 +43,7 @@ def c1_view(seed: int = 1):
 import json
 import math
 import os
-from decimal import Decimal, getcontext
+from decimal import Context, Decimal, getcontext
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DATA = os.path.join(HERE, "views_data.json")
@@ -145,6 +145,138 @@ def c3_views(seed: int = 3, n: int = 64, size_div: int = 1):
     return out
 
 
+# The learned-scheduling workload: a 7680x4320 image with uniform 3x3
+# supersampling, rendered as 23040x12960 samples with sub 1; half-width 1e-500,
+# maxiter 2e6. Its minibrot is the period-38045 nucleus stored in
+# views_data.json ("c4", size 3.2e-501: the minibrot spans about a third of
+# the view's width; it is the copy of the standard set's period-5 real-axis
+# minibrot inside a period-7609
+# minibrot found by a seeded search next to the C2 nucleus). The view is
+# centred 1e-3 of the view width outward from a point of that minibrot's edge:
+# the boundary pixel nearest a seed-drawn point of the estimated main cardioid
+# (nucleus + size (e/2 - e^2/4)), refined by renders at shrinking half-widths
+# (c4_edge_search, which needs a GPU), so the edge crosses the image near its
+# centre.
+C4_W, C4_H, C4_HW_LOG10, C4_MXIT = 23040, 12960, -500, 2_000_000
+
+
+def c4_cardioid_point(seed: int = 4):
+    """Estimated edge point: nucleus + size (e/2 - e^2/4), e = exp(i th) with
+    th seed-drawn away from the cusp."""
+    d = nucleus()["c4"]
+    rng = np.random.RandomState(seed)
+    th = rng.uniform(0.25 * math.pi, 1.75 * math.pi)
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    sre, sim = Decimal(d["size_re"]), Decimal(d["size_im"])
+    e = complex(math.cos(th), math.sin(th))
+    card = e / 2 - e * e / 4
+    ere = Decimal(d["nucleus_re"]) + sre * Decimal(repr(card.real)) - sim * Decimal(repr(card.imag))
+    eim = Decimal(d["nucleus_im"]) + sre * Decimal(repr(card.imag)) + sim * Decimal(repr(card.real))
+    return ere, eim
+
+
+def c4_view():
+    """Centre, half-width and pitch of the whole C4 image (decimals)."""
+    d = nucleus()["c4"]
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    hw = Decimal(10) ** C4_HW_LOG10
+    nx, ny = d["edge_normal"]
+    cre = Decimal(d["edge_re"]) + Decimal("1e-3") * 2 * hw * Decimal(repr(nx))
+    cim = Decimal(d["edge_im"]) + Decimal("1e-3") * 2 * hw * Decimal(repr(ny))
+    return {"center_re": cre, "center_im": cim, "hw": hw, "pitch": 2 * hw / (C4_W - 1), "width": C4_W, "height": C4_H,
+            "max_iterations": C4_MXIT, "bailout": 256.0, "period": d["period"]}
+
+
+def c4_edge_search(be, seed: int = 4, n: int = 512, levels: int = 8):
+    """The boundary of the C4 minibrot near its seed-drawn cardioid point:
+    render n x n at maxiter 2e6 around the current point, take the boundary
+    pixel (non-escaping, with an escaping 4-neighbour) nearest it, divide the
+    half-width by 32, repeat down to a half-width below 1e-502. Returns the
+    edge point and its outward normal (exterior minus interior pixel means in
+    a 9x9 window)."""
+    import mbx
+
+    d = nucleus()["c4"]
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    sre, sim = Decimal(d["size_re"]), Decimal(d["size_im"])
+    tre, tim = c4_cardioid_point(seed)
+    cre, cim = Decimal(d["nucleus_re"]), Decimal(d["nucleus_im"])
+    hw = 2 * (sre * sre + sim * sim).sqrt()
+    res = None
+    for _ in range(levels):
+        scale = format(Context(prec=30).divide(Decimal(2), hw), "E").replace("E+", "e")
+        r = mbx.ComputeRequest(format(cre, "f"), format(cim, "f"), scale, n, n, C4_MXIT, bailout=256.0, precision_bits=2000,
+                               precision_mode=mbx.PRECISION_MIXED, reference_re=d["nucleus_re"], reference_im=d["nucleus_im"],
+                               reference_period=d["period"])
+        if be.compute_status(r) != mbx.OK:
+            raise RuntimeError(be.last_error())
+        it = r.iterations.reshape(n, n)
+        inside = (it < 0) | (it >= C4_MXIT - 1)
+        pitch = 2 * hw / (n - 1)
+        c0re, c0im = cre - hw, cim - hw
+        out = np.zeros_like(inside)
+        out[1:, :] |= ~inside[:-1, :]
+        out[:-1, :] |= ~inside[1:, :]
+        out[:, 1:] |= ~inside[:, :-1]
+        out[:, :-1] |= ~inside[:, 1:]
+        bd = np.argwhere(inside & out)
+        if len(bd) == 0:
+            break
+        tx, ty = float((tre - c0re) / pitch), float((tim - c0im) / pitch)
+        py, px = bd[np.argmin((bd[:, 1] - tx) ** 2 + (bd[:, 0] - ty) ** 2)]
+        cre, cim = c0re + pitch * Decimal(int(px)), c0im + pitch * Decimal(int(py))
+        tre, tim = cre, cim
+        y0, y1, x0, x1 = max(0, py - 4), min(n, py + 5), max(0, px - 4), min(n, px + 5)
+        yy, xx = np.mgrid[y0:y1, x0:x1]
+        w = inside[y0:y1, x0:x1]
+        v = np.array([xx[~w].mean() - xx[w].mean(), yy[~w].mean() - yy[w].mean()])
+        v = v / np.linalg.norm(v)
+        res = dict(edge_re=format(cre, "f"), edge_im=format(cim, "f"), edge_normal=[float(v[0]), float(v[1])],
+                   edge_pitch_log10=float(pitch.log10()))
+        if float(hw.log10()) < C4_HW_LOG10 - 2:
+            break
+        hw = hw / 32
+    return res
+
+
+def c4_tiles(seed: int = 4, n: int = 32, tile: int = 256):
+    """n seed-drawn tile x tile tiles of the C4 image (without repeats), each a
+    view with the image's pixel pitch, its centre at the tile's centre. Every
+    tile names the C4 nucleus as its periodic reference (one orbit for all)."""
+    v = c4_view()
+    d = nucleus()["c4"]
+    getcontext().prec = len(d["nucleus_re"]) + 20
+    nx, ny = C4_W // tile, C4_H // tile
+    rng = np.random.RandomState(seed)
+    picks = rng.permutation(nx * ny)[:n]
+    p = v["pitch"]
+    # pixel (x, y) of the image sits at c0 + x pitch + i y pitch
+    c0re = v["center_re"] - p * Decimal(C4_W - 1) / 2
+    c0im = v["center_im"] - p * Decimal(C4_H - 1) / 2
+    hw_t = p * Decimal(tile - 1) / 2
+    scale = format(Context(prec=30).divide(Decimal(2), hw_t), "E").replace("E+", "e")
+    out = []
+    for k in picks.tolist():
+        ty, tx = divmod(int(k), nx)
+        cre = c0re + p * (Decimal(tx * tile) + Decimal(tile - 1) / 2)
+        cim = c0im + p * (Decimal(ty * tile) + Decimal(tile - 1) / 2)
+        out.append({
+            "center_re": format(cre, "f"),
+            "center_im": format(cim, "f"),
+            "scale": scale,
+            "width": tile,
+            "height": tile,
+            "max_iterations": C4_MXIT,
+            "bailout": 256.0,
+            "precision_bits": int(-C4_HW_LOG10 * math.log2(10)) + 128,
+            "reference_re": d["nucleus_re"],
+            "reference_im": d["nucleus_im"],
+            "reference_period": d["period"],
+            "label": "c4-%d-%d" % (tx, ty),
+        })
+    return out
+
+
 # Frames with committed arbitrary-precision truth subsets (tests/golden/make_truth.py).
 TRUTH_FRAMES = ("1e-300", "1e-1000", "1e-1000-minibrot")
 
@@ -175,6 +307,50 @@ if __name__ == "__main__":
         d["zoom"].update(nucleus_re=nre, nucleus_im=nim, period=p, size_log10=ls)
         json.dump(d, open(DATA, "w"), indent=1)
         print("period", p, "size 1e%.2f" % ls)
+    if "--regenerate-c4" in sys.argv:
+        import mbx
+        import mpmath
+
+        def complex_size(nre, nim, p):
+            """1 / (beta lambda^2) over one period."""
+            mpmath.mp.prec = 2400
+            c = mpmath.mpc(mpmath.mpf(nre), mpmath.mpf(nim))
+            z, lam, beta = mpmath.mpc(0), mpmath.mpc(1), mpmath.mpc(1)
+            for _ in range(1, p):
+                z = z * z + c
+                lam = 2 * z * lam
+                beta = beta + 1 / lam
+            s = 1 / (beta * lam * lam)
+            return mpmath.nstr(s.real, 20), mpmath.nstr(s.imag, 20)
+
+        d = nucleus()
+        getcontext().prec = len(d["nucleus_re"]) + 40
+        rng = np.random.RandomState(4004)
+        phi = rng.uniform(0, 2 * math.pi)
+        r = Decimal(10) ** -250
+        cre = Decimal(d["nucleus_re"]) + r * Decimal(repr(math.cos(phi)))
+        cim = Decimal(d["nucleus_im"]) + r * Decimal(repr(math.sin(phi)))
+        p, nre, nim, ls = mbx.find_nucleus(format(cre, "f"), format(cim, "f"), "3e-251", 200000, 2400)
+        sre, sim = complex_size(nre, nim, p)
+        parent = dict(nucleus_re=nre, nucleus_im=nim, period=p, size_log10=ls, size_re=sre, size_im=sim)
+        # the parent's copy of the period-5 minibrot on the real axis of the standard set
+        x = Decimal("-1.985424253054205")
+        cre = Decimal(nre) + Decimal(sre) * x
+        cim = Decimal(nim) + Decimal(sim) * x
+        mag = (Decimal(sre) ** 2 + Decimal(sim) ** 2).sqrt()
+        p, nre, nim, ls = mbx.find_nucleus(format(cre, "f"), format(cim, "f"), format(mag * Decimal("1e-4"), "E"), 400000, 2400)
+        sre, sim = complex_size(nre, nim, p)
+        d["c4"] = dict(nucleus_re=nre, nucleus_im=nim, period=p, size_log10=ls, size_re=sre, size_im=sim, parent=parent)
+        json.dump(d, open(DATA, "w"), indent=1)
+        print("period", p, "size 1e%.2f" % ls)
+    if "--regenerate-c4-edge" in sys.argv:
+        import mbx
+
+        be = mbx.create_compute_backend("cuda")
+        d = nucleus()
+        d["c4"].update(c4_edge_search(be))
+        be.close()
+        json.dump(d, open(DATA, "w"), indent=1)
     if "--regenerate-minibrot" in sys.argv:
         import mbx
 
