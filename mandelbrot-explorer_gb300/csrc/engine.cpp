@@ -274,7 +274,7 @@ void Engine::release_device() {
     for (void* p : {(void*)dZ_.p, (void*)dZfe_.p, (void*)dD_.p, (void*)dzm3_.p, (void*)dr2_.p, (void*)dab_.p, (void*)dce_.p,
                     (void*)ddcx_.p, (void*)ddcy_.p, (void*)diter_own_.p, (void*)dnormal_own_.p, (void*)descN_own_.p, (void*)dkeys_.p,
                     (void*)dglitch_.p, (void*)ddone_.p, (void*)dgmp_.p, (void*)dflags_.p, (void*)dZf_.p, (void*)dZq_.p, (void*)dZsmall_.p, (void*)dbla32_.p, (void*)dblamax_.p,
-                    (void*)drerun_keys_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p,
+                    (void*)drerun_keys_.p, (void*)drerun_flag_.p, (void*)dflag_sums_.p, (void*)drerun_done_.p, (void*)drerun_gmp_.p, (void*)drerun2_keys_.p, (void*)dbladf_.p, (void*)dZdf_.p,
                     (void*)dcost_.p, (void*)dblac_.p, (void*)dpgrid_.p, (void*)ddpxy_.p, (void*)ddpxyf_.p})
         if (p) cudaFree(p);
     if (dctr_) cudaFree(dctr_);
@@ -1508,7 +1508,8 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         kept.swap(*keys);
     }
     if (n <= 0) return MBX_OK;
-    if (!ensure(ddone_, n) || !ensure(drerun_keys_, n) || !ensure(drerun2_keys_, n) || !ensure(drerun_done_, n) || !ensure(drerun_gmp_, n))
+    if (!ensure(ddone_, n) || !ensure(drerun_keys_, n) || !ensure(drerun2_keys_, n) || !ensure(drerun_done_, n) || !ensure(drerun_gmp_, n) ||
+        !ensure(drerun_flag_, n) || !ensure(dflag_sums_, flag_blocks((unsigned)n) + 1))
         return MBX_E_NOMEM;
     cudaMemsetAsync(ddone_.p, 0, n, st_);
     cudaMemsetAsync(dctr_, 0, 2 * sizeof(Counters), st_);
@@ -1516,6 +1517,12 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
     DeviceFrame f = frame_view();
     f.px = px;
     f.rerun_keys = drerun_keys_.p;
+    // the main pass flags its leftovers; they are queued in entry order after
+    // it (neighbouring samples in a warp, rather than the order they failed in)
+    if (!probe_gate_only_) {
+        cudaMemsetAsync(drerun_flag_.p, 0, n, st_);
+        f.rerun_flag = drerun_flag_.p;
+    }
     const double t0 = now_ms();
     cudaEventRecord(ev0_, st_);
     cudaError_t e = run_mixed_pass(f);
@@ -1560,6 +1567,9 @@ int Engine::run_pass_mixed(std::vector<uint64_t>* keys, const PixelSet& grid, in
         r.rerun_keys = next_q;
         return r;
     };
+    e = launch_flag_compact(px, (unsigned)n, drerun_flag_.p, dflag_sums_.p, drerun_keys_.p, st_);
+    if (e != cudaSuccess) return fail_cuda("rerun queue compaction", e);
+    stats_.kernel_launches += 3;
     e = run_df_pass(queue_frame(drerun_keys_.p, 0, drerun2_keys_.p, 1));
     stats_.kernel_launches += 2; // narrow and wide variants, one of which runs
     if (e != cudaSuccess) return fail_cuda("double-float rerun launch", e);

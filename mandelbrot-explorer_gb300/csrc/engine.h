@@ -239,6 +239,8 @@ class Engine {
     int dpxy_w_ = 0;
     bool probe_gate_only_ = false; // mixed form: the gate's probe pass runs its FP32 tier only
     DevBuf<uint64_t> drerun_keys_;            // mixed pass: queue for the double-float pass
+    DevBuf<uint8_t> drerun_flag_;             // mixed main pass: per entry, left to the double-float pass
+    DevBuf<unsigned> dflag_sums_;             // block sums of their compaction
     DevBuf<uint64_t> drerun2_keys_;           // double-float pass: samples it cannot vouch for (the exact form finishes them)
     DevBuf<uint8_t> drerun_done_, drerun_gmp_; // flags of that pass, by queue position
     bool exact_rerun_ = false; // mixed form: the FP64 floatexp rerun of flagged samples is running

@@ -199,6 +199,7 @@ struct DeviceFrame {
     Counters* ctr;
     volatile int* cancel;    // host-mapped flag
     uint64_t* rerun_keys = nullptr; // mixed pass: queue of sample keys for the FP64 floatexp pass
+    uint8_t* rerun_flag = nullptr;  // mixed FP32 pass: per entry, set when left to the next tier (then compacted in entry order)
 };
 
 // Launchers (kernels_exact.cu).
@@ -303,5 +304,7 @@ cudaError_t launch_batch_gate(ViewDesc* views, int n, const unsigned* view_inter
 // by view, rows of samples): sums holds flag_blocks(total) words
 unsigned flag_blocks(unsigned total);
 cudaError_t launch_flag_compact(const ViewDesc* views, int nv, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st);
+// the same over one pass's entries (keys in entry order)
+cudaError_t launch_flag_compact(const PixelSet& px, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st);
 
 } // namespace mbx

@@ -235,10 +235,14 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
             } else if (LaneReal<T>::kTrackError && st >= 3) { // queued for the next tier
                 if (st == 4) ++n_intflag;
                 if (st == 5) ++n_escflag;
-                int a[4];
-                entry_coords(f.px, L.i, a);
                 const unsigned q = atomicAdd(&f.ctr->rerun_n, 1u);
-                f.rerun_keys[q] = key_pack(a[0], a[1], a[2], a[3]);
+                if (f.rerun_flag) {
+                    f.rerun_flag[L.i] = 1; // queued in entry order after the pass
+                } else {
+                    int a[4];
+                    entry_coords(f.px, L.i, a);
+                    f.rerun_keys[q] = key_pack(a[0], a[1], a[2], a[3]);
+                }
                 f.out.done[L.i] = 1;
                 ++n_fin;
                 live = false;
@@ -689,7 +693,32 @@ __global__ void __launch_bounds__(1024) k_flag_scan(unsigned nb, unsigned* sums)
         base += c;
     }
 }
-__global__ void __launch_bounds__(1024) k_flag_emit(const ViewDesc* views, int nv, const uint8_t* flag, unsigned total, const unsigned* sums, uint64_t* out) {
+// keys of flagged samples: batch-wide indices over views, or a pass's entries
+struct ViewsKeys {
+    const ViewDesc* views;
+    int nv;
+    __device__ uint64_t operator()(unsigned g) const {
+        int lo = 0, hi = nv - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (views[mid].base <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        int arr[4];
+        entry_coords(views[lo].f.px, (int)(g - views[lo].base), arr);
+        return key_pack(arr[0], arr[1], arr[2], arr[3]) | ((uint64_t)lo << kBatchViewShift);
+    }
+};
+struct EntryKeys {
+    PixelSet px;
+    __device__ uint64_t operator()(unsigned g) const {
+        int arr[4];
+        entry_coords(px, (int)g, arr);
+        return key_pack(arr[0], arr[1], arr[2], arr[3]);
+    }
+};
+template <class Keys>
+__global__ void __launch_bounds__(1024) k_flag_emit(Keys keys, const uint8_t* flag, unsigned total, const unsigned* sums, uint64_t* out) {
     __shared__ unsigned ws[32];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned g0 = blockIdx.x * kFlagBlock + threadIdx.x * 4;
@@ -717,28 +746,24 @@ __global__ void __launch_bounds__(1024) k_flag_emit(const ViewDesc* views, int n
     }
     __syncthreads();
     unsigned pos = sums[blockIdx.x] + (warp ? ws[warp - 1] : 0u) + x - c;
-    for (int k = 0; k < 4; ++k) {
-        if (!f[k]) continue;
-        const unsigned g = g0 + k;
-        int lo = 0, hi = nv - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (views[mid].base <= g) lo = mid;
-            else hi = mid - 1;
-        }
-        int arr[4];
-        entry_coords(views[lo].f.px, (int)(g - views[lo].base), arr);
-        out[pos++] = key_pack(arr[0], arr[1], arr[2], arr[3]) | ((uint64_t)lo << kBatchViewShift);
-    }
+    for (int k = 0; k < 4; ++k)
+        if (f[k]) out[pos++] = keys(g0 + k);
 }
 
-cudaError_t launch_flag_compact(const ViewDesc* views, int nv, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st) {
+template <class Keys>
+cudaError_t flag_compact(Keys keys, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st) {
     const unsigned nb = flag_blocks(total);
     if (nb == 0) return cudaSuccess;
     k_flag_sums<<<nb, 1024, 0, st>>>(flag, total, sums);
     k_flag_scan<<<1, 1024, 0, st>>>(nb, sums);
-    k_flag_emit<<<nb, 1024, 0, st>>>(views, nv, flag, total, sums, out);
+    k_flag_emit<<<nb, 1024, 0, st>>>(keys, flag, total, sums, out);
     return cudaGetLastError();
+}
+cudaError_t launch_flag_compact(const ViewDesc* views, int nv, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st) {
+    return flag_compact(ViewsKeys{views, nv}, total, flag, sums, out, st);
+}
+cudaError_t launch_flag_compact(const PixelSet& px, unsigned total, const uint8_t* flag, unsigned* sums, uint64_t* out, cudaStream_t st) {
+    return flag_compact(EntryKeys{px}, total, flag, sums, out, st);
 }
 
 cudaError_t launch_batch_gate(ViewDesc* views, int n, const unsigned* view_interior, cudaStream_t st) {

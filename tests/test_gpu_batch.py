@@ -42,7 +42,7 @@ def test_batch_matches_single_frames():
         rc = be.compute_batch(reqs)
         assert rc == mbx.OK, be.last_error()
         bs = be.last_batch_stats.as_dict()
-        assert bs["kernel_launches"] == 8 and bs["passes"] == 2  # probe, gate, main, regrouping (3), double-float (2)
+        assert bs["kernel_launches"] == 8 and bs["passes"] == 2  # probe, gate, main, leftover compaction (3), double-float (2)
         for (it, en), r, (v, w, h) in zip(singles, reqs, frames):
             assert np.array_equal(r.escape_iteration, en), (rep, w, h)
             assert np.array_equal(r.iterations, it), (rep, w, h)
