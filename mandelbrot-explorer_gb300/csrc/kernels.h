@@ -174,7 +174,7 @@ struct FeParams {
     int no_bla_kernel;       // mp.cpp:2185-2193 solveRescaledSimd8NoBla semantics
     int ref_period_gt0;
     int cutoff_sensitive;
-    int one_lane_per_warp = 0; // few long samples (the mixed form's last tier): one per warp, no divergence between them
+    int lanes_per_warp = 0;  // exact-form leftovers: lanes of each warp that take samples (0: all 32)
 };
 
 // Shallow direct loop (mp.cpp:330-532).

@@ -833,7 +833,7 @@ __device__ PixOut pixel_fe_nobla(const DeviceFrame& f, const FeParams& p, FE dcr
 }
 
 __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
-    if (p.one_lane_per_warp && (threadIdx.x & 31u)) return;
+    if (p.lanes_per_warp && (int)(threadIdx.x & 31u) >= p.lanes_per_warp) return;
     const FrameGeom& g = p.g;
     unsigned long long n_steps = 0, n_bla = 0, n_skip = 0, n_eff = 0;
     unsigned int n_int = 0;
