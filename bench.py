@@ -121,6 +121,33 @@ def cpu_reference(views_list, sample_w, sample_h, threads):
     return eff / dt / 1e9, dt, eff
 
 
+def profile_c4(args):
+    """args.profile_c4 tiles of the learned-scheduling image (256x256 each) as
+    one batch, warmup + steps times, the model ordering and training (probe
+    cells, prediction, ordering, shared passes, tcgen05 training)."""
+    import mbx
+    import order_train
+    import views
+
+    tiles = views.c4_tiles(n=args.profile_c4)
+    be = mbx.create_compute_backend("cuda")
+    order_train.load_weights(be)
+    assert be.set_batch_scheduling(1) == mbx.OK, be.last_error()
+    times = []
+    for k in range(args.warmup + args.steps):
+        reqs = [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], v["width"], v["height"], v["max_iterations"], bailout=v["bailout"],
+                                   precision_bits=v["precision_bits"], precision_mode=mbx.PRECISION_MIXED, reference_re=v["reference_re"],
+                                   reference_im=v["reference_im"], reference_period=v["reference_period"]) for v in tiles]
+        t = time.perf_counter()
+        assert be.compute_batch(reqs) == mbx.OK, be.last_error()
+        if k >= args.warmup:
+            times.append((time.perf_counter() - t) * 1e3)
+    st = be.last_batch_stats.as_dict()
+    be.close()
+    print(json.dumps({"profile_c4": {"tiles": len(tiles), "ms": float(np.mean(times)), "shared_passes_gpu_ms": st["pass_gpu_ms"],
+                                     "fp32_pass_gpu_ms": st["fp32_pass_gpu_ms"], "kernel_launches": st["kernel_launches"]}}))
+
+
 def profile_run(args, vlist):
     """A small, fixed launch sequence for profilers: each listed view rendered
     warmup + steps times in the mixed form with the default launch shape and a
@@ -178,9 +205,15 @@ def main():
     ap.add_argument("--plain-sample", default="full", help="plain FP64 GPU sample size (same views), WxH or 'full' (the frames' own size)")
     ap.add_argument("--profile", default=None, help="comma-separated view labels (e.g. 1e-300): render (and colour) only those, default launch shape, no baselines (for ncu captures)")
     ap.add_argument("--profile-batch", action="store_true", help="with --profile: render the views as one batch with the learned ordering training")
+    ap.add_argument("--profile-c4", type=int, default=0, help="render N tiles of the learned-scheduling image as one batch with the model training on it (for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    import order_train
     import views
+
+    if args.profile_c4:
+        profile_c4(args)
+        return
 
     vlist = views.c2_views(width=args.width, height=args.height) + [views.minibrot_view(width=args.width, height=args.height)]
     sw, sh = (int(x) for x in args.cpu_sample.split("x"))
@@ -472,6 +505,54 @@ def main():
     c3_line = {"views": len(c3), "sample": "all 64 seed-drawn views at 1/8 of their linear sizes (32..512 square; 32 with 3x3 adaptive supersampling), references resident",
                "ms_per_batch": c3_t / args.steps * 1e3, "shared_graph_gpu_ms": c3_gpu / args.steps, "gpixel_iter_per_s": c3_eff / c3_t / 1e9, "unit": UNIT}
 
+    # learned-scheduling workload (views.c4_tiles): 24 seed-drawn 256x256 tiles
+    # of the 23040x12960 image (7680x4320 with 3x3 uniform supersampling) at
+    # half-width 1e-500 by a period-38045 minibrot's edge, maxiter 2e6, as one
+    # mbx_compute_batch per step: natural order, the untrained model (tiles by
+    # mean probe cost), and the committed weights trained further on the batch
+    c4 = views.c4_tiles(n=24)
+    c4be = mbx.create_compute_backend("cuda", local)
+
+    def c4_reqs():
+        return [mbx.ComputeRequest(v["center_re"], v["center_im"], v["scale"], v["width"], v["height"], v["max_iterations"], bailout=v["bailout"],
+                                   precision_bits=v["precision_bits"], precision_mode=mbx.PRECISION_MIXED, reference_re=v["reference_re"],
+                                   reference_im=v["reference_im"], reference_period=v["reference_period"]) for v in c4]
+
+    def c4_time(k):
+        t_, eff_, f32_, g_, out_ = 0.0, 0, 0.0, 0.0, None
+        for _ in range(k):
+            rq = c4_reqs()
+            t = time.perf_counter()
+            assert c4be.compute_batch(rq) == mbx.OK, c4be.last_error()
+            t_ += time.perf_counter() - t
+            bs_ = c4be.last_batch_stats
+            eff_ += bs_.effective_iterations + sum(s_.effective_iterations for s_ in c4be.last_view_stats)
+            f32_ += bs_.fp32_pass_gpu_ms
+            g_ += bs_.pass_gpu_ms
+            out_ = [r.escape_iteration.copy() for r in rq]
+        return {"ms_per_batch": t_ / k * 1e3, "fp32_pass_gpu_ms": f32_ / k, "shared_graph_gpu_ms": g_ / k, "gpixel_iter_per_s": eff_ / t_ / 1e9}, out_
+
+    c4_init = order_train.initial_params()
+    c4be.set_batch_scheduling(0)
+    c4_time(1)  # the engines' orbits and tables
+    c4_nat, c4_o0 = c4_time(args.steps)
+    c4be.schedule_params(c4_init)
+    c4be.set_batch_scheduling(2)
+    c4_time(1)
+    c4_un, c4_o1 = c4_time(args.steps)
+    order_train.load_weights(c4be)
+    c4be.set_batch_scheduling(1)
+    c4_time(1)  # trains on this batch's map
+    c4be.set_batch_scheduling(2)
+    c4_tr, c4_o2 = c4_time(args.steps)
+    c4be.close()
+    c4_samples = sum(v["width"] * v["height"] for v in c4)
+    c4_line = {"tiles": len(c4), "sample": "24 seed-drawn 256x256 tiles (%d samples) of the 23040x12960 image; half-width 1e-500, maxiter 2e6" % c4_samples,
+               "natural": c4_nat, "untrained_model": c4_un, "trained_model": c4_tr, "unit": UNIT,
+               "identical_outputs": all(np.array_equal(a, b) and np.array_equal(a, c) for a, b, c in zip(c4_o0, c4_o1, c4_o2)),
+               "full_image_s_at_trained_rate": c4_tr["ms_per_batch"] / 1e3 * (views.C4_W * views.C4_H) / c4_samples,
+               "model": "order_model_params.npz (trained offline on C1/C2 maps by order_train.py), 32 Adam steps on the batch"}
+
     # plain FP64 GPU form on a sample of the same views, and accuracy vs it
     if args.plain_sample == "full":
         pw, ph = W, H
@@ -561,6 +642,7 @@ def main():
                 "image_epilogue": epilogue,
                 "zoom_sequence": zoom_line,
                 "batch_c3": c3_line,
+                "learned_order_c4": c4_line,
                 "reruns_per_frame": reruns,
             },
             "e2e": {"value": e2e_batch_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": eb_t / 2 * 1e3,

@@ -630,22 +630,23 @@ __global__ void __launch_bounds__(128) k_grad(const float* P, const __nv_bfloat1
     }
 }
 
-// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the summed gradients.
-__global__ void k_adam(float* P, float* M, float* V, const float* grad, int* step_count, int* ready, float lr) {
-    const int it = *step_count + 1;
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the summed gradients: step k of
+// a training call (the call's first step follows the *step_count taken before).
+__global__ void k_adam(float* P, float* M, float* V, const float* grad, const int* step_count, int k, float lr) {
+    const int it = *step_count + k + 1;
     const float c1 = 1.0f - powf(0.9f, (float)it), c2 = 1.0f - powf(0.999f, (float)it);
-    for (int k = threadIdx.x; k < SchedLayout::N; k += blockDim.x) {
-        const float g = grad[k];
-        const float m = 0.9f * M[k] + 0.1f * g, v = 0.999f * V[k] + 0.001f * g * g;
-        M[k] = m;
-        V[k] = v;
-        P[k] -= lr * (m / c1) / (sqrtf(v / c2) + 1e-8f);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        *step_count = it;
-        *ready = 1;
-    }
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= SchedLayout::N) return;
+    const float g = grad[j];
+    const float m = 0.9f * M[j] + 0.1f * g, v = 0.999f * V[j] + 0.001f * g * g;
+    M[j] = m;
+    V[j] = v;
+    P[j] -= lr * (m / c1) / (sqrtf(v / c2) + 1e-8f);
+}
+// after a training call's steps
+__global__ void k_adam_done(int* step_count, int* ready, int steps) {
+    *step_count += steps;
+    *ready = 1;
 }
 
 // Initial weights: hidden unit 0 of both layers carries feature 15 (the mean
@@ -728,8 +729,9 @@ cudaError_t sched_train(SchedState& s, const ViewDesc* main, int nv, unsigned nt
         cudaMemsetAsync(s.grad, 0, sizeof(float) * SchedLayout::N, st);
         k_grad<<<kTrainBlocks, kRows, sizeof(TrainSmem), st>>>(s.params, s.X, s.T, n, (int)(((long long)k * rows) % n), rows, s.grad,
                                                               k + 1 == steps ? s.loss : nullptr, s.err);
-        k_adam<<<1, 256, 0, st>>>(s.params, s.adam_m, s.adam_v, s.grad, s.steps, s.ready, lr);
+        k_adam<<<(SchedLayout::N + 255) / 256, 256, 0, st>>>(s.params, s.adam_m, s.adam_v, s.grad, s.steps, k, lr);
     }
+    k_adam_done<<<1, 1, 0, st>>>(s.steps, s.ready, steps);
     return cudaGetLastError();
 }
 
@@ -741,6 +743,6 @@ cudaError_t sched_gradient(SchedState& s, const __nv_bfloat16* X, const float* T
     return cudaGetLastError();
 }
 
-int sched_train_launches(int steps) { return 1 + 2 * steps; }
+int sched_train_launches(int steps) { return 2 + 2 * steps; }
 
 } // namespace mbx
