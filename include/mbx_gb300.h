@@ -15,7 +15,7 @@
 extern "C" {
 #endif
 
-#define MBX_ABI_VERSION 3
+#define MBX_ABI_VERSION 4
 
 /* Coloring flags: same bit values as the reference's ColoringMethod enum
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
@@ -139,14 +139,21 @@ typedef struct {
     int smem_orbit_limit;   /* stage the FP32 orbit into shared memory when it fits in this many bytes (0: never) */
     double rescale_window;  /* |w|^2 is kept in [1/window, window]; 1e4 to 1e16 */
     double pass_ms;         /* autotune: GPU time of the calibration pass with this shape */
+    int lane_budget;        /* iterations a lane walks per call between its warp's refill points: 16 to 4096 */
 } mbx_tuning;
 
 /* Sets the mixed-pass tuning of a context (values out of range are ignored). */
 int mbx_set_tuning(mbx_context* ctx, int threads, int blocks_per_sm, int smem_orbit_limit, double rescale_window);
 
+/* Sets the iterations a mixed-pass lane walks per call between its warp's
+ * refill points (16 to 4096; the span of the orbit a warp covers between
+ * refills; results do not depend on it). */
+int mbx_set_lane_budget(mbx_context* ctx, int iterations);
+
 /* Autotuner: renders `calibration` (a floatexp frame) in mixed precision once
  * per candidate (block size x resident blocks x orbit staging x rescale
- * window), keeps the fastest shape on the context and returns it in *best. */
+ * window x lane span between refills), keeps the fastest shape on the context
+ * and returns it in *best. */
 int mbx_autotune(mbx_context* ctx, const mbx_request* calibration, mbx_tuning* best);
 
 /* Diagnostic: measured issue rate of dependent-free FMA chains on the context's

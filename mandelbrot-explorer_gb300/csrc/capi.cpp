@@ -197,6 +197,14 @@ int mbx_set_tuning(mbx_context* c, int threads, int blocks_per_sm, int smem_orbi
     return MBX_OK;
 }
 
+int mbx_set_lane_budget(mbx_context* c, int iterations) {
+    if (!c) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    c->engine->set_lane_budget(iterations);
+    return MBX_OK;
+}
+
 int mbx_autotune(mbx_context* c, const mbx_request* calib, mbx_tuning* best) {
     if (!c || !calib) return MBX_E_INVALID;
     std::string why;
@@ -224,13 +232,16 @@ int mbx_autotune(mbx_context* c, const mbx_request* calib, mbx_tuning* best) {
     const int blocks_opts[] = {2, 3, 4};
     const int smem_opts[] = {200 * 1024, 0};
     const double window_opts[] = {1e8, 1e12, 1e16};
+    const int budget_opts[] = {64, 256, 1024};
     double best_ms = 1e300;
     mbx_tuning b = {};
     for (int t : threads_opts)
         for (int bl : blocks_opts)
             for (int sm : smem_opts)
-                for (double w : window_opts) {
+                for (double w : window_opts)
+                    for (int lb : budget_opts) {
                     c->engine->set_tuning(t, bl, sm, (float)w);
+                    c->engine->set_lane_budget(lb);
                     double ms = 1e300;
                     for (int rep = 0; rep < 2; ++rep) {
                         rc = c->engine->compute(r, &st);
@@ -247,9 +258,11 @@ int mbx_autotune(mbx_context* c, const mbx_request* calib, mbx_tuning* best) {
                         b.smem_orbit_limit = sm;
                         b.rescale_window = w;
                         b.pass_ms = ms;
+                        b.lane_budget = lb;
                     }
-                }
+                    }
     c->engine->set_tuning(b.threads, b.blocks_per_sm, b.smem_orbit_limit, (float)b.rescale_window);
+    c->engine->set_lane_budget(b.lane_budget);
     if (best) *best = b;
     return MBX_OK;
 }

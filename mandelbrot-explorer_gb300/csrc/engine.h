@@ -260,6 +260,7 @@ class Engine {
     int mixed_threads_ = 256;
     int mixed_blocks_per_sm_ = 3;
     int smem_orbit_limit_ = 0;
+    int lane_budget_ = 256;
     float mixed_wmax2_ = 1e16f;
 
   public:
@@ -269,6 +270,10 @@ class Engine {
         if (smem_limit >= 0 && smem_limit <= 220 * 1024) smem_orbit_limit_ = smem_limit;
         if (wmax2 >= 1e4f && wmax2 <= 1e16f) mixed_wmax2_ = wmax2;
     }
+    void set_lane_budget(int n) {
+        if (n >= 16 && n <= 4096) lane_budget_ = n;
+    }
+    int lane_budget() const { return lane_budget_; }
     void get_tuning(int* threads, int* blocks_per_sm, int* smem_limit, float* wmax2) const {
         *threads = mixed_threads_;
         *blocks_per_sm = mixed_blocks_per_sm_;

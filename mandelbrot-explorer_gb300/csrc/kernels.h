@@ -232,6 +232,7 @@ struct MixedParams {
     float esc2lo = 0.0f;
     const uint8_t* Zsmall;   // 1 where |Z| is below FP32 normal range (use the floatexp shadow)
     int orbit_in_smem;       // stage the whole (periodic) orbit into shared memory
+    int lane_budget = 256;   // iterations (orbit entries) a lane walks per call between its warp's refill points
     int smem_entries;
     float wmax2, wmin2;      // |w|^2 rescale window
     // Per supersampled column / row: the sample's offset from the reference in

@@ -123,11 +123,12 @@ __device__ bool stage_orbit(float2* smem, const float2* g, int entries, unsigned
     return mbar_wait_bounded(mb, 1 << 22);
 }
 
-// Iterations a lane takes per lane_run call between the warp's refill points.
-// Longer calls amortise the warp's reconvergence and refill (measured on the
-// 1080p 1e-300 frame: FP32 passes 6.0 ms at 32, 5.4 at 128, 4.6 at 256, 4.7
-// at 1024); finished lanes return at once and wait for the warp's next refill.
-constexpr int kLaneBudget = 256;
+// Iterations a lane takes per lane_run call between the warp's refill points
+// (MixedParams::lane_budget, a tuning axis: the span of the orbit a warp walks
+// between refills). Longer calls amortise the warp's reconvergence and refill
+// (measured on the 1080p 1e-300 frame: FP32 passes 6.0 ms at 32, 5.4 at 128,
+// 4.6 at 256, 4.7 at 1024); finished lanes return at once and wait for the
+// warp's next refill. Where a call ends changes no result.
 
 // The lane pass, persistent: warps pull samples from the pass's work counter
 // and refill idle lanes together. T = float is the mixed pass (orbit staged in
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_lane_pass(DeviceFrame f, MixedPa
         }
         if (live) {
             T zrad = T(0);
-            const int st = lane_run<T, INTR, FASTI, DE>(L, kLaneBudget, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
+            const int st = lane_run<T, INTR, FASTI, DE>(L, p.lane_budget, f, p, bt, orb, reflen, ESC2f, blamask, zrad, n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             if (p.probe_stop && (st == 2 || st == 4)) atomicExch(&f.ctr->probe_hit, 1u);
             if (st != 0 && f.out.cost) f.out.cost[L.oidx] = (unsigned)(n_steps + 4 * n_bla) - cost0;
             if (st == 1) {
@@ -362,7 +363,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch_pass(BatchArgs a) {
             const ViewDesc& vd = a.views[view];
             const BlaEntry<T>* bt = vd.f.bla.use ? ViewTables<T>::bla(vd) : nullptr;
             T zrad = T(0);
-            const int st = lane_run<T, true, false, DE>(L, kLaneBudget, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, T(vd.p.esc2f), (1 << vd.f.bla.minlevel) - 1, zrad,
+            const int st = lane_run<T, true, false, DE>(L, vd.p.lane_budget, vd.f, vd.p, bt, ViewTables<T>::orb(vd), vd.p.mx_ref_it + 1, T(vd.p.esc2f), (1 << vd.f.bla.minlevel) - 1, zrad,
                                                        n_steps, n_bla, n_skip, n_rebase, n_exact, n_ferebase);
             // the learned ordering's costs: the FP32 tier's (the rerun tiers keep them)
             if (std::is_same<T, float>::value && st != 0 && vd.f.out.cost) {
@@ -557,6 +558,7 @@ MixedParams Engine::mixed_params() const {
         p.dpx_tabf = ddpxyf_.p;
         p.dpy_tabf = ddpxyf_.p + dpxy_w_;
     }
+    p.lane_budget = lane_budget_;
     return p;
 }
 

@@ -79,6 +79,7 @@ class Tuning(ctypes.Structure):
         ("smem_orbit_limit", ctypes.c_int),
         ("rescale_window", ctypes.c_double),
         ("pass_ms", ctypes.c_double),
+        ("lane_budget", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -144,6 +145,7 @@ EXPORTS = (
     "mbx_measure_fma_peak",
     "mbx_render_shallow_noalloc",
     "mbx_set_tuning",
+    "mbx_set_lane_budget",
     "mbx_autotune",
     "mbx_compute_batch",
     "mbx_set_batch_scheduling",
@@ -220,6 +222,8 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_measure_fma_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.mbx_set_tuning.restype = ctypes.c_int
         lib.mbx_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        lib.mbx_set_lane_budget.restype = ctypes.c_int
+        lib.mbx_set_lane_budget.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.mbx_autotune.restype = ctypes.c_int
         lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
         lib.mbx_set_batch_scheduling.restype = ctypes.c_int
@@ -375,6 +379,12 @@ class CudaComputeBackend:
         rc = self._lib.mbx_set_tuning(self._ctx, threads, blocks_per_sm, smem_orbit_limit, rescale_window)
         if rc != OK:
             raise RuntimeError("set_tuning failed (%d)" % rc)
+
+    def set_lane_budget(self, iterations: int):
+        """Iterations a mixed-pass lane walks per call between refills."""
+        rc = self._lib.mbx_set_lane_budget(self._ctx, int(iterations))
+        if rc != OK:
+            raise RuntimeError("set_lane_budget failed (%d)" % rc)
 
     def compute_status(self, req: ComputeRequest) -> int:
         r, _keep = self._build(req)

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = mbx.load_library()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.mbx_abi_version() == 3
+    assert lib.mbx_abi_version() == 4
 
 
 def test_no_cpu_fallback_without_device():

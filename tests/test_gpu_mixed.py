@@ -173,6 +173,32 @@ ANGLE_P999 = 1e-4    # normal map: 99.9th percentile of |d angle| (radians, mod 
 ANGLE_MAX = 1e-3
 
 
+def test_lane_budget_changes_no_result():
+    """The autotuner's lane-span axis (iterations a lane walks per call between
+    its warp's refill points) changes only where calls end: the outputs of a
+    frame whose samples take every tier, with and without interior detection
+    and with the derivative, are bit-identical at 64, 256 and 1024."""
+    cases = load_cases()
+    be = mbx.create_compute_backend("cuda")
+    try:
+        for name, cm in (("minibrot875", None), ("subpixel737", None), ("minibrot875", 1)):
+            c = cases[name]
+            ref = None
+            for lb in (256, 64, 1024):
+                be.set_lane_budget(lb)
+                req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], sub=c["sub"],
+                                         coloring_method=c["coloring_method"] if cm is None else cm, bailout=c["bailout"],
+                                         precision_mode=mbx.PRECISION_MIXED)
+                assert be.compute_status(req) == mbx.OK, be.last_error()
+                out = (req.iterations.copy(), req.escape_iteration.copy())
+                if ref is None:
+                    ref = out
+                else:
+                    assert np.array_equal(out[0], ref[0]) and np.array_equal(out[1], ref[1]), (name, cm, lb)
+    finally:
+        be.close()
+
+
 def _de_errors(values, n, tv, tn, angle, skip=None):
     ok = (n == tn) & (tn > 0) & (values > -5)
     if skip is not None:
