@@ -21,7 +21,9 @@ extern "C" {
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
 #define MBX_SUPER_SAMPLING 1
 #define MBX_EXTERIOR_DIST_EST 2
+#define MBX_STRIPE_AVERAGE 8 /* value = stripe average over the last 256 iterations (src/engine/orbit_coloring.h:21-95); sub 1, exact form */
 #define MBX_NORMAL_MAP 16 /* value = smooth iteration; normal buffer = arg(z) - arg(dz/dc) (mp.cpp:375-378, 2489-2492, 3512-3515) */
+#define MBX_ORBIT_TRAP 32 /* value = 0.17 (-log10 trap distance) + 0.025 mu (orbit_coloring.h:97-132); interior samples carry it too; sub 1, exact form */
 #define MBX_DE_OVERLAY 64
 
 /* What a request renders (ComputeMode, src/engine/compute_backend.h:18). */
@@ -30,7 +32,7 @@ extern "C" {
 
 /* Arithmetic of the per-sample delta loop. */
 #define MBX_PRECISION_EXACT 0 /* FP64 / FP64-floatexp in the reference's exact operation order */
-#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration with rebasing, for every perturbation frame (scale > 1e6) without DE colouring; others take the exact form */
+#define MBX_PRECISION_MIXED 1 /* FP32-mantissa floatexp bulk iteration with rebasing, for every perturbation frame (scale > 1e6), DE colourings included; shallow frames and the orbit colourings (SAC, traps) take the exact form */
 
 /* Status codes (the reference returns bool + ComputeBackendInfo strings). */
 #define MBX_OK 0

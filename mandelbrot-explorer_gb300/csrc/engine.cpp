@@ -9,6 +9,7 @@
 // to be. Citations: cbotx/Mandelbrot-Explorer src/engine/mandel_perturbation.cpp
 // ("mp.cpp"), src/engine/bigfixed.h, src/engine/float_math.cpp.
 #include "engine.h"
+#include "orbit_color.h"
 #include "parmul.h"
 
 #include <algorithm>
@@ -442,6 +443,12 @@ float Engine::gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) c
     mpf_set(z_im, c_im);
     mpf_set_str(d_re, "2", 10);
     const bool ede = (cm_ & 2) != 0;
+    // orbit colourings on the arbitrary-precision orbit (mp.cpp:763-770, 819-820)
+    const bool sac = (cm_ & 8) != 0, trap = (cm_ & 32) != 0;
+    StripeAvg sacc;
+    OrbitTrap trapc;
+    if (sac) sacc.init();
+    if (trap) trapc.init();
     mpf_set_ui(dc_re, 1);
     float res = -2;
     for (int i = 1; i < mxit; ++i) {
@@ -471,6 +478,8 @@ float Engine::gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) c
         mpf_add(z_re, z_re, c_re);
         mpf_mul_ui(z_im, a1, 2);
         mpf_add(z_im, z_im, c_im);
+        if (sac) sacc.push(mpf_get_d(z_re), mpf_get_d(z_im));
+        if (trap) trapc.push(mpf_get_d(z_re), mpf_get_d(z_im));
         mpf_mul(a1, z_re, z_re);
         mpf_mul(a2, z_im, z_im);
         mpf_add(a1, a1, a2);
@@ -491,6 +500,10 @@ float Engine::gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) c
                     res = (float)mpf_get_d(e1);
                 } else
                     res = 0.f;
+            } else if (sac) { // here the stripe average takes precedence (mp.cpp:851-863)
+                res = sacc.value(rad, (double)escf_);
+            } else if (trap) {
+                res = trapc.value((double)i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2));
             } else {
                 res = (float)(i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2));
             }
@@ -502,6 +515,7 @@ float Engine::gmp_point(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int* nout) c
         if (mpf_get_d(a1) < 0.000000001) break;
         if ((i & 255) == 0 && cancel_.load()) return kEmpty;
     }
+    if (trap && res == -2.0f) res = trapc.value(0.0); // mp.cpp:882
     return res;
 }
 
@@ -657,7 +671,9 @@ int Engine::build_reference(const int* pick, bool view_center) {
     if (!escaped) {
         if (ref_virtual_ && use_floatexp_) fe_cutoff_sensitive_ = gmp_point(ref_re_, ref_im_, MXIT_ + 64, nullptr) >= 0;
         if (!ref_virtual_) {
-            ref_value_ = -2.0f;
+            // an orbit trap colours interior samples too: the reference pixel's
+            // value from its arbitrary-precision orbit (mp.cpp:4179-4184)
+            ref_value_ = (cm_ & 32) ? gmp_point(ref_re_, ref_im_, MXIT_, nullptr) : -2.0f;
             ref_n_ = -1;
             ref_value_pending_ = true;
         }
@@ -1465,6 +1481,8 @@ FrameGeom Engine::geom() const {
     g.deovl = (cm_ & 64) ? 1 : 0;
     g.deriv = deriv_ ? 1 : 0;
     g.normal = (cm_ & 16) ? 1 : 0;
+    g.oc = ((cm_ & 8) ? kOcStripe : 0) | ((cm_ & 32) ? kOcTrap : 0);
+    g.ER = (double)escf_;
     return g;
 }
 
@@ -1482,7 +1500,8 @@ FeParams Engine::fe_params(int mx_ref_it) const {
     p.interior_confirm = interior_confirm_;
     p.interior_eps2 = interior_eps2_;
     p.fused = 1;
-    p.no_bla_kernel = (!use_bla_ && !deriv_) ? 1 : 0;
+    // the reference's no-BLA lane kernel has no derivative and no orbit colourings (mp.cpp:2148)
+    p.no_bla_kernel = (!use_bla_ && !deriv_ && !(cm_ & (8 | 32))) ? 1 : 0;
     p.ref_period_gt0 = ref_period_ > 0 ? 1 : 0;
     p.cutoff_sensitive = fe_cutoff_sensitive_ ? 1 : 0;
     return p;
@@ -2409,7 +2428,7 @@ int Engine::render_shallow(volatile float* progress) {
     p.c0i = mpf_ld(c0_im_);
     p.dx = mpf_ld(dx_);
     p.dy = mpf_ld(dy_);
-    p.simd_semantics = (cm_ & (16 | 64)) ? 0 : 1; // the normal map and the DE overlay take the scalar path (mp.cpp:1455-1459)
+    p.simd_semantics = (cm_ & (8 | 16 | 32 | 64)) ? 0 : 1; // SAC, the normal map, traps and the DE overlay take the scalar path (mp.cpp:1455-1459)
     PixelSet g;
     g.keys = nullptr;
     g.grid_w = W_;

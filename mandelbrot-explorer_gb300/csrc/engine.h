@@ -248,7 +248,8 @@ class Engine {
     void fill_batch_slot();
     int batch_ref_it_ = 0; // reference length of the deferred frame's passes
     // The FP32 pass carries no derivative: DE colourings take the exact form.
-    bool mixed_active() const { return mode_ == MBX_PRECISION_MIXED; }
+    // the mixed form renders every perturbation frame except orbit colourings (SAC, traps: exact form)
+    bool mixed_active() const { return mode_ == MBX_PRECISION_MIXED && !(cm_ & (8 | 32)); }
 
     // mixed-pass launch shape (set by the autotuner / defaults: orbit read
     // through L1, the choice of the autotuner on both 1080p deep frames).

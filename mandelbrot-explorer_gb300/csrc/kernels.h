@@ -143,6 +143,8 @@ struct FrameGeom {
     double dxf;       // mpf_get_ld(_dx)
     int ede, deovl, deriv;
     int normal;       // normal map: arg(z) - arg(dz/dc) into the normal buffer (EDE takes precedence)
+    int oc = 0;       // orbit colourings (orbit_color.h): kOcStripe | kOcTrap (exact form only)
+    double ER = 0.0;  // escape radius as the reference keeps it: (double)(float R)
 };
 
 // Double-precision delta loop parameters (mp.cpp:2290-2585).

@@ -8,6 +8,7 @@
 // Reference: cbotx/Mandelbrot-Explorer src/engine/mandel_perturbation.cpp
 // ("mp.cpp"); the per-pixel semantics are those of its scalar loops.
 #include "kernels.h"
+#include "orbit_color.h"
 
 namespace mbx {
 
@@ -63,6 +64,10 @@ __device__ __forceinline__ int bla_try_fp64(const BlaView& b, const double2* Z, 
     return 0;
 }
 
+// OC: the orbit colourings (orbit_color.h): their accumulators take every
+// iteration's z; a trap turns BLA and the state-repetition detector off
+// (mp.cpp:2121, 2388), a BLA skip restarts the stripe window (:2422-2427).
+template <int OC>
 __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) {
     const FrameGeom& g = p.g;
     const double2* Z = f.orbit.Z;
@@ -105,7 +110,9 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
         int conf_P = 0, conf_next = 0, conf_count = 0, conf_giveup = 0;
         double conf_D2 = 0, conf_zr = 0, conf_zi = 0;
         const bool detect = p.use_interior != 0;
-        const bool int_rep = p.int_rep && detect;
+        const bool int_rep = p.int_rep && detect && !(OC & kOcTrap);
+        OrbitColor<OC> oc;
+        oc.init();
         double sdzr = 1e300, sdzi = 1e300;
         int sk = -1, save_j2 = j, twin2 = 1;
         int outcome = 0; // 0 running, 1 escaped, 2 interior, 3 glitch
@@ -129,7 +136,7 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
                     twin2 += twin2;
                 }
             }
-            if (f.bla.use && dzr * dzr + dzi * dzi < f.bla.rmax2) {
+            if (f.bla.use && !(OC & kOcTrap) && dzr * dzr + dzi * dzi < f.bla.rmax2) {
                 int skip = bla_try_fp64(f.bla, Z, rkm1, dzr, dzi, ddr, ddi, dcr, dci, g.deriv, g.ESC2, p.mx_ref_it);
                 if (skip > 0) {
                     ++n_bla;
@@ -139,6 +146,7 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
                     rk += skip;
                     if (per && rk >= per) rk -= per;
                     rkm1 = (per && rk == 0) ? per - 1 : rk - 1;
+                    oc.skipped();
                     zsr = 1e30;
                     zsi = 1e30;
                     save_j = j;
@@ -178,6 +186,7 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
             zr = dzr + zc.x;
             zi = dzi + zc.y;
             zrad = zr * zr + zi * zi;
+            oc.push(zr, zi);
             ++k;
             rkm1 = rk;
             if (per) {
@@ -263,8 +272,10 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
                 if (g.normal) {
                     // normal angle arg(z) - arg(dz/dc) (mp.cpp:2489-2492)
                     if (f.out.normal) f.out.normal[idx] = (float)(atan2(zi, zr) - atan2(di, dr));
-                } else if (g.deovl && f.out.normal) {
-                    f.out.normal[idx] = (float)(sqrt(zrad) / g.dxf * log(zrad) / sqrt(dr * dr + di * di));
+                } else if (g.deovl) {
+                    if (f.out.normal) f.out.normal[idx] = (float)(sqrt(zrad) / g.dxf * log(zrad) / sqrt(dr * dr + di * di));
+                } else if (OC) { // trap, else stripe average (mp.cpp:2497-2500)
+                    v = oc.escaped(smooth_value(j + 1, zrad), zrad, g.ER);
                 }
             }
             f.out.iter[idx] = v;
@@ -272,7 +283,7 @@ __global__ void __launch_bounds__(128) k_fp64_pass(DeviceFrame f, Fp64Params p) 
             f.out.done[i] = 1;
             n_eff += (unsigned long long)(j + 1);
         } else if (outcome == 2) {
-            f.out.iter[idx] = -2.0f;
+            f.out.iter[idx] = oc.interior();
             if (f.out.escN) f.out.escN[idx] = -1;
             f.out.done[i] = 1;
             n_eff += (unsigned long long)g.mxit;
@@ -452,6 +463,9 @@ struct PixOut {
 };
 
 // pixelRescaled (mp.cpp:3287-3618), smooth / EDE / DE-overlay.
+// OC: the orbit colourings, as in k_fp64_pass (mp.cpp:3338-3346, 3389-3397,
+// 3503-3504, 3524-3529); a trap turns BLA off.
+template <int OC>
 __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE dci, unsigned long long& n_steps, unsigned long long& n_bla, unsigned long long& n_skip) {
     const FrameGeom& g = p.g;
     const double2* Z = f.orbit.Z;
@@ -481,7 +495,9 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
     FE SJ = fe_make(1.0, 0);
     double jr = 1.0, ji = 0.0, invSJd = 1.0;
     const bool detect = p.use_interior != 0;
-    const bool int_rep = p.int_rep && detect;
+    const bool int_rep = p.int_rep && detect && !(OC & kOcTrap);
+    OrbitColor<OC> oc;
+    oc.init();
     double swr = 1e300, swi = 1e300;
     FE sS = fe_make(1e300, 0);
     int sm = -1, save_iter2 = 1, twin2r = 1;
@@ -509,12 +525,13 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 twin2r += twin2r;
             }
         }
-        if (f.bla.use && m >= 2) {
+        if (f.bla.use && !(OC & kOcTrap) && m >= 2) {
             double ab[4];
             int skip = bla_try_fe(f.bla, Z, p.ref_period_gt0, rm, S, S2, wr, wi, dr, di, g.ESC2, per ? per : reflen, deriv ? ab : nullptr);
             if (skip > 0) {
                 ++n_bla;
                 n_skip += skip;
+                oc.skipped();
                 if (deriv) {
                     FE Jr = fe_mul_d(SJ, jr), Ji = fe_mul_d(SJ, ji);
                     FE nJr = fe_add(fe_sub(fe_mul_d(Jr, ab[0]), fe_mul_d(Ji, ab[1])), fe_from(ab[2]));
@@ -611,6 +628,7 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
         Xi = X.y;
         double zr = Xr + s * wr, zi = Xi + s * wi;
         double zrad = zr * zr + zi * zi;
+        oc.push(zr, zi);
         if (zrad > g.ESC2) {
             o.n = iter;
             o.state = 1;
@@ -627,6 +645,9 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 double num = sqrt(zrad) * log(zrad);
                 FE Jmag = fe_mul_d(SJ, sqrt(jr * jr + ji * ji));
                 o.nrm = (float)fe_to_double(fe_div(fe_from(num), fe_mul(p.dxfe, Jmag)));
+            } else if (OC) { // trap, else stripe average
+                o.value = oc.escaped((double)iter - log(log(zrad) / 2.0 / kLn2) / kLn2, zrad, g.ER);
+                return o;
             }
             o.value = (float)((double)iter - log(log(zrad) / 2.0 / kLn2) / kLn2);
             return o;
@@ -639,7 +660,7 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                     double pr = zr - conf_zr, pi = zi - conf_zi;
                     if (pr * pr + pi * pi < p.interior_eps2 * zrad && conf_D2 < 1.0) {
                         if (++conf_count >= p.interior_confirm) {
-                            o.value = -2.0f;
+                            o.value = oc.interior();
                             o.state = 2;
                             return o;
                         }
@@ -709,7 +730,7 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
             }
         }
     }
-    o.value = -2.0f;
+    o.value = oc.interior();
     o.state = 2;
     return o;
 }
@@ -832,6 +853,7 @@ __device__ PixOut pixel_fe_nobla(const DeviceFrame& f, const FeParams& p, FE dcr
     }
 }
 
+template <int OC>
 __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
     if (p.lanes_per_warp && (int)(threadIdx.x & 31u) >= p.lanes_per_warp) return;
     const FrameGeom& g = p.g;
@@ -851,7 +873,8 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
         double py = arr[0] + (double)arr[2] / g.sub;
         FE Dcr = fe_mul_d(p.dxfe, px - p.ref_x);
         FE Dci = fe_mul_d(p.dyfe, py - p.ref_y);
-        PixOut o = p.no_bla_kernel ? pixel_fe_nobla(f, p, Dcr, Dci, n_steps) : pixel_fe(f, p, Dcr, Dci, n_steps, n_bla, n_skip);
+        // (the no-BLA lane kernel has no orbit colourings, mp.cpp:2148)
+        PixOut o = (OC == 0 && p.no_bla_kernel) ? pixel_fe_nobla(f, p, Dcr, Dci, n_steps) : pixel_fe<OC>(f, p, Dcr, Dci, n_steps, n_bla, n_skip);
         if (o.state == 4) break;
         const int idx = sample_index(g, arr);
         // mp.cpp:2173-2183: EMPTY or cutoff-sensitive results go to the
@@ -882,9 +905,12 @@ __global__ void __launch_bounds__(128) k_fe_pass(DeviceFrame f, FeParams p) {
 // ---------------------------------------------------------------------------
 // Shallow direct loop: floatPointCompute (mp.cpp:330-399) and the lane-refill
 // kernel's per-lane arithmetic (mp.cpp:416-532).
+template <int OC>
 __device__ double shallow_scalar(double c_re, double c_im, int mxit, const FrameGeom& g, double* nrm, int* nout) {
     double z_re = c_re, z_im = c_im, d_re = 2, d_im = 0, dc_re = 1, dc_im = 0, tmp;
     const bool deriv = g.ede || g.deovl || g.normal;
+    OrbitColor<OC> oc; // mp.cpp:347-369
+    oc.init();
     int i = 1;
     while (i < mxit) {
         tmp = 2.0 * (d_re * z_re - d_im * z_im);
@@ -898,6 +924,7 @@ __device__ double shallow_scalar(double c_re, double c_im, int mxit, const Frame
         tmp = z_re * z_re - z_im * z_im + c_re;
         z_im = 2.0 * z_re * z_im + c_im;
         z_re = tmp;
+        oc.push(z_re, z_im);
         tmp = z_re * z_re + z_im * z_im;
         if (tmp > g.ESC2) {
             *nout = i + 1;
@@ -906,14 +933,18 @@ __device__ double shallow_scalar(double c_re, double c_im, int mxit, const Frame
                 if (nrm) *nrm = atan2(z_im, z_re) - atan2(dc_im, dc_re);
                 return (i + 1 - log(log(tmp) / 2 / kLn2) / kLn2);
             }
-            if (g.deovl && nrm) *nrm = sqrt(tmp) * log(tmp) / sqrt(dc_re * dc_re + dc_im * dc_im);
+            if (g.deovl) {
+                if (nrm) *nrm = sqrt(tmp) * log(tmp) / sqrt(dc_re * dc_re + dc_im * dc_im);
+                return (i + 1 - log(log(tmp) / 2 / kLn2) / kLn2);
+            }
+            if (OC) return oc.escaped(i + 1 - log(log(tmp) / 2 / kLn2) / kLn2, tmp, g.ER); // mp.cpp:383-389
             return (i + 1 - log(log(tmp) / 2 / kLn2) / kLn2);
         }
         tmp = d_re * d_re + d_im * d_im;
-        if (tmp < 0.000000001) return -2;
+        if (tmp < 0.000000001) return oc.interior();
         ++i;
     }
-    return -2;
+    return oc.interior();
 }
 
 __device__ float shallow_lane(double cr, double ci, int mxit, const FrameGeom& g, int* nout) {
@@ -1017,6 +1048,7 @@ __global__ void __launch_bounds__(128) k_julia(DeviceFrame f, JuliaParams p) {
 
 // Base pass (mp.cpp:1483-1519) in grid mode, or adaptive-SS sub-samples
 // (mp.cpp:1920-1969) from a key list.
+template <int OC>
 __global__ void __launch_bounds__(128) k_shallow(DeviceFrame f, ShallowParams p) {
     const FrameGeom& g = p.g;
     unsigned long long n_eff = 0, n_steps = 0;
@@ -1038,13 +1070,13 @@ __global__ void __launch_bounds__(128) k_shallow(DeviceFrame f, ShallowParams p)
         const int idx = sample_index(g, arr);
         int nout = -1;
         double val;
-        if (p.simd_semantics) {
+        if (OC == 0 && p.simd_semantics) { // (no orbit colourings in the lane kernel, mp.cpp:1459)
             val = (double)shallow_lane(cr, ci, g.mxit, g, &nout);
             if (g.ede && val >= 0) val /= p.dx;
             f.out.iter[idx] = (float)val;
         } else {
             double de = 0.0;
-            val = shallow_scalar(cr, ci, g.mxit, g, &de, &nout);
+            val = shallow_scalar<OC>(cr, ci, g.mxit, g, &de, &nout);
             if (g.normal) { // mp.cpp:1504-1507 (with EDE also set: the raw distance, angle 0)
                 f.out.iter[idx] = (float)val;
                 if (f.out.normal) f.out.normal[idx] = (float)de;
@@ -1052,9 +1084,10 @@ __global__ void __launch_bounds__(128) k_shallow(DeviceFrame f, ShallowParams p)
                 float v = (float)val;
                 f.out.iter[idx] = v;
                 if (f.out.normal) f.out.normal[idx] = (v < 0) ? 0.0f : (float)(de / p.dx);
-            } else {
-                if (g.ede && val >= 0) val /= p.dx;
-                f.out.iter[idx] = (float)val;
+            } else { // the value is stored as float before the EDE division (mp.cpp:1512-1515)
+                float v = (float)val;
+                if (g.ede && v >= 0) v = (float)((double)v / p.dx);
+                f.out.iter[idx] = v;
             }
         }
         if (f.out.escN) f.out.escN[idx] = nout;
@@ -1175,11 +1208,21 @@ cudaError_t launch_fill(float* iter, float* normal, int32_t* escN, size_t n, cud
     return cudaGetLastError();
 }
 cudaError_t launch_fp64_pass(const DeviceFrame& f, const Fp64Params& p, int blocks, int threads, cudaStream_t st) {
-    k_fp64_pass<<<blocks, threads, 0, st>>>(f, p);
+    switch (p.g.oc) {
+    case 0: k_fp64_pass<0><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcStripe: k_fp64_pass<kOcStripe><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcTrap: k_fp64_pass<kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    default: k_fp64_pass<kOcStripe | kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_fe_pass(const DeviceFrame& f, const FeParams& p, int blocks, int threads, cudaStream_t st) {
-    k_fe_pass<<<blocks, threads, 0, st>>>(f, p);
+    switch (p.g.oc) {
+    case 0: k_fe_pass<0><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcStripe: k_fe_pass<kOcStripe><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcTrap: k_fe_pass<kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    default: k_fe_pass<kOcStripe | kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_julia(const DeviceFrame& f, const JuliaParams& p, int blocks, int threads, cudaStream_t st) {
@@ -1188,7 +1231,12 @@ cudaError_t launch_julia(const DeviceFrame& f, const JuliaParams& p, int blocks,
 }
 
 cudaError_t launch_shallow(const DeviceFrame& f, const ShallowParams& p, int blocks, int threads, cudaStream_t st) {
-    k_shallow<<<blocks, threads, 0, st>>>(f, p);
+    switch (p.g.oc) {
+    case 0: k_shallow<0><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcStripe: k_shallow<kOcStripe><<<blocks, threads, 0, st>>>(f, p); break;
+    case kOcTrap: k_shallow<kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    default: k_shallow<kOcStripe | kOcTrap><<<blocks, threads, 0, st>>>(f, p); break;
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_bla_build(const double2* Z, const double2* D, int reflen, double eps, double dcmax, bool ede, double* r2, double4* ab, double4* ce, const int* off, const int* size, int nlev, unsigned long long* rmax2_bits, cudaStream_t st) {

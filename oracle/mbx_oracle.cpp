@@ -4,7 +4,7 @@
 // renderer. Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline /
 // reference legs may load it; the product never does.
 //
-// Scope: Mandel::Compute for coloring flags {0, SUPER_SAMPLING, EXTERIOR_DIST_EST,
+// Scope: Mandel::Compute for coloring flags {0, SUPER_SAMPLING, EXTERIOR_DIST_EST, STRIPE_AVERAGE, ORBIT_TRAP,
 // DE_OVERLAY} with the reference's default engine switches (BLA on, interior
 // detection on, floatexp gate at scale > 1e280, periodic reference auto,
 // BigFixed auto, fused rescaled step). The per-pixel loops follow the scalar
@@ -35,7 +35,69 @@
 namespace {
 
 constexpr float EMPTY = -10.0f; // mp.h:23 EMPTYPIXEL
-constexpr int CM_SS = 1, CM_EDE = 2, CM_NORMAL = 16, CM_DEOVL = 64; // mp.h:30-49
+constexpr int CM_SS = 1, CM_EDE = 2, CM_SAC = 8, CM_NORMAL = 16, CM_TRAP = 32, CM_DEOVL = 64; // mp.h:30-49
+
+// Orbit colourings (src/engine/orbit_coloring.h:21-132): the stripe average
+// over a triangular window of the last 256 terms 1/2 + sin(7 arg z)/2, and the
+// orbit traps (min distance to 0, the cross weighted 1.5, the circle |z| = 1/2).
+struct OrbitAcc {
+    static constexpr int W = 256;
+    bool sac = false, trap = false;
+    double ring[W];
+    double RS = 0, TS = 0, last = 0;
+    int pos = 0, fill = 0;
+    double minP = 1e300, minX = 1e300, minC = 1e300;
+    void init(int cm) {
+        sac = (cm & CM_SAC) != 0;
+        trap = (cm & CM_TRAP) != 0;
+        RS = TS = last = 0;
+        pos = fill = 0;
+        minP = minX = minC = 1e300;
+    }
+    void push(double zr, double zi) {
+        if (sac) {
+            double t = 0.5 + 0.5 * std::sin(7.0 * std::atan2(zi, zr));
+            last = t;
+            double ev = fill == W ? ring[pos] : (++fill, 0.0);
+            TS += (double)W * t - RS;
+            RS += t - ev;
+            ring[pos] = t;
+            pos = (pos + 1) % W;
+        }
+        if (trap) {
+            double m2 = zr * zr + zi * zi;
+            if (m2 < minP) minP = m2;
+            double x = std::min(std::fabs(zr), std::fabs(zi));
+            if (x < minX) minX = x;
+            double c = std::fabs(std::sqrt(m2) - 0.5);
+            if (c < minC) minC = c;
+        }
+    }
+    void skipped() { // a BLA jump breaks the stripe window
+        if (sac) {
+            RS = TS = 0;
+            pos = fill = 0;
+        }
+    }
+    float sacValue(double zrad, double radius) const {
+        double f = 1.0 - std::log(std::log(zrad) * 0.5 / std::log(radius)) / std::log(2.0);
+        double w = (double)fill * W - (double)fill * (fill - 1) / 2.0;
+        double inc = w > 0.0 ? TS / w : 0.0;
+        double exc = w > (double)W ? (TS - (double)W * last) / (w - (double)W) : inc;
+        f -= std::floor(f);
+        return (float)(exc + (inc - exc) * f);
+    }
+    float trapValue(double mu) const {
+        double d = std::min(std::min(std::sqrt(minP), minX * 1.5), minC);
+        if (d > 1.0) d = 1.0;
+        double tr = -std::log10(std::max(d, 1e-14));
+        if (mu < 0.0) mu = 0.0;
+        return (float)(0.17 * tr + 0.025 * mu);
+    }
+    // the loops' escape value when no DE/normal/overlay colouring applies: trap first
+    float escaped(double mu, double zrad, double radius) const { return trap ? trapValue(mu) : sacValue(zrad, radius); }
+    float interior() const { return trap ? trapValue(0.0) : -2.0f; }
+};
 constexpr int SA_N = 30;                            // mp.h:288
 
 // ---------------------------------------------------------------------------
@@ -460,6 +522,9 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
     const bool de_ovl = (cm & CM_DEOVL) != 0;
     const bool normal = (cm & CM_NORMAL) != 0;
     const bool deriv = (cm & CM_EDE) || normal || de_ovl;
+    OrbitAcc oc; // mp.cpp:347-351
+    oc.init(cm);
+    const bool ocol = oc.sac || oc.trap;
     int i = 1;
     while (i < mxit) {
         tmp = 2.0 * (d_re * z_re - d_im * z_im);
@@ -473,6 +538,7 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
         tmp = z_re * z_re - z_im * z_im + c_re;
         z_im = 2.0 * z_re * z_im + c_im;
         z_re = tmp;
+        if (ocol) oc.push((double)z_re, (double)z_im);
         tmp = z_re * z_re + z_im * z_im;
         if (tmp > ESC2) {
             if (nout) *nout = i + 1;
@@ -485,13 +551,14 @@ double Engine::floatPoint(double c_re, double c_im, int mxit, int cm, double* nr
                 if (nrm) *nrm = std::sqrt(tmp) * std::log(tmp) / std::sqrt(dc_re * dc_re + dc_im * dc_im);
                 return (i + 1 - std::log(std::log(tmp) / 2 / std::log(2)) / std::log(2));
             }
+            if (ocol) return oc.escaped(i + 1 - std::log(std::log(tmp) / 2 / std::log(2)) / std::log(2), (double)tmp, (double)escf); // mp.cpp:383-389
             return (i + 1 - std::log(std::log(tmp) / 2 / std::log(2)) / std::log(2));
         }
         tmp = d_re * d_re + d_im * d_im;
-        if (tmp < 0.000000001) return -2;
+        if (tmp < 0.000000001) return oc.interior();
         ++i;
     }
-    return -2;
+    return oc.interior();
 }
 
 // mp.cpp:416-532 for one pixel (lane refill does not change per-pixel values).
@@ -542,6 +609,8 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
     const bool angle = !ede && (cm & kTruthAngle) != 0;
     mpf_init2(dc_re, wp); mpf_set_ui(dc_re, 1);
     mpf_init2(dc_im, wp); mpf_init2(e1, wp); mpf_init2(e2, wp);
+    OrbitAcc oc; // mp.cpp:763-770 (the stripe average takes precedence at escape here, :851-863)
+    oc.init(cm);
     int i = 1;
     float res = -2;
     while (i < mxit) {
@@ -571,6 +640,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
         mpf_add(z_re, z_re, c_re);
         mpf_mul_ui(z_im, tt1, 2);
         mpf_add(z_im, z_im, c_im);
+        oc.push(mpf_get_d(z_re), mpf_get_d(z_im)); // mp.cpp:819-820
         mpf_mul(tt1, z_re, z_re);
         mpf_mul(tt2, z_im, z_im);
         mpf_add(tt1, tt1, tt2);
@@ -607,6 +677,10 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
                     res = (float)mpf_get_d(e1);
                 } else
                     res = 0.f;
+            } else if (oc.sac) {
+                res = oc.sacValue(rad, (double)escf);
+            } else if (oc.trap) {
+                res = oc.trapValue((double)i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2));
             } else {
                 res = (i + 1 - std::log(std::log(rad) / 2 / std::log(2)) / std::log(2));
             }
@@ -619,6 +693,7 @@ float Engine::accuratePoint(mpf_srcptr c_re, mpf_srcptr c_im, int mxit, int cm, 
         if (rad < 0.000000001) break;
         ++i;
     }
+    if (oc.trap && res == -2.0f) res = oc.trapValue(0.0); // mp.cpp:882
     mpf_clears(tt1, tt2, z_re, z_im, d_re, d_im, dc_re, dc_im, e1, e2, (mpf_ptr)0);
     return res;
 }
@@ -1079,7 +1154,7 @@ int Engine::createRef(std::set<std::array<int, 4>>& s, int pr_it, int mxit, bool
         }
     }
     if (ref_virtual && use_floatexp) fe_cutoff_sensitive = accuratePoint(ref_re, ref_im, mxit + 64, cm) >= 0;
-    if (!ref_virtual) setPixel(ref_, -2.f, -1);
+    if (!ref_virtual) setPixel(ref_, (cm & CM_TRAP) ? accuratePoint(ref_re, ref_im, mxit, cm) : -2.f, -1); // mp.cpp:4179-4184
     return mxit;
 }
 
@@ -1491,7 +1566,9 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
     FE SJ{1.0, 0};
     double jr = 1.0, ji = 0.0, invSJd = 1.0;
     const bool detect_interior = use_interior;
-    const bool int_rep = opt.int_rep > 0 && detect_interior;
+    OrbitAcc oc; // mp.cpp:3338-3346, 3365-3366
+    oc.init(cm);
+    const bool int_rep = opt.int_rep > 0 && detect_interior && !oc.trap;
     double swr = 1e300, swi = 1e300;
     FE sS{1e300, 0};
     int sm = -1, save_iter2 = 1, twin2r = 1;
@@ -1507,10 +1584,11 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
                 twin2r += twin2r;
             }
         }
-        if (use_bla && m >= 2) {
+        if (use_bla && !oc.trap && m >= 2) { // mp.cpp:3389
             double ab[4];
             int skip = tryBLAfe(rm, S, S2, wr, wi, dr, di, per ? per : reflen, deriv ? ab : nullptr);
             if (skip > 0) {
+                oc.skipped(); // mp.cpp:3393-3397
                 if (deriv) {
                     FE Jr = fe_mul_d(SJ, jr), Ji = fe_mul_d(SJ, ji);
                     FE nJr = fe_add(fe_sub(fe_mul_d(Jr, ab[0]), fe_mul_d(Ji, ab[1])), fe_from(ab[2]));
@@ -1604,6 +1682,7 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
         Xi = m ? zfi[rm] : 0.0;
         double zr = Xr + s * wr, zi = Xi + s * wi;
         double zrad = zr * zr + zi * zi;
+        oc.push(zr, zi); // mp.cpp:3503-3504
         if (zrad > ESC2) {
             *nout = iter;
             if (ede) {
@@ -1621,6 +1700,7 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
                 if (nrm) *nrm = (float)fe_to_double(fe_div(fe_from(num), fe_mul(dxfe, Jmag)));
                 return (float)((double)iter - std::log(std::log(zrad) / 2.0 / LG2) / LG2);
             }
+            if (oc.sac || oc.trap) return oc.escaped((double)iter - std::log(std::log(zrad) / 2.0 / LG2) / LG2, zrad, (double)escf); // mp.cpp:3524-3529
             return (float)((double)iter - std::log(std::log(zrad) / 2.0 / LG2) / LG2);
         }
         if (detect_interior) {
@@ -1630,7 +1710,7 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
                 if (iter >= conf_next) {
                     double pr = zr - conf_zr, pi = zi - conf_zi;
                     if (pr * pr + pi * pi < interior_eps2 * zrad && conf_D2 < 1.0) {
-                        if (++conf_count >= interior_confirm) return -2.f;
+                        if (++conf_count >= interior_confirm) return oc.interior();
                         conf_zr = zr;
                         conf_zi = zi;
                         conf_D2 = 1;
@@ -1697,7 +1777,7 @@ float Engine::pixelRescaled(FE dcr, FE dci, int mx_ref_it, int mxit, int cm, flo
             }
         }
     }
-    return -2.f;
+    return oc.interior();
 }
 
 // mp.cpp:3620-3816 for one lane (lanes are independent).
@@ -1815,7 +1895,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
     const bool deriv = ede || normal || de_ovl;
     long long steps = 0, blas = 0, skipped = 0, gmp = 0;
     if (use_floatexp) {
-        const bool noBla = !use_bla && !deriv;
+        const bool noBla = !use_bla && !deriv && !(cm & (CM_SAC | CM_TRAP)); // mp.cpp:2148
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : gmp)
         for (int i = 0; i < n; ++i) {
             const Pix arr = P(v[i]);
@@ -1887,7 +1967,9 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
         int conf_P = 0, conf_next = 0, conf_count = 0, conf_giveup = 0;
         double conf_D2 = 0, conf_zr = 0, conf_zi = 0;
         const bool detect_interior = use_interior;
-        const bool int_rep = opt.int_rep > 0 && detect_interior;
+        OrbitAcc oc; // mp.cpp:2362-2364, 2387-2388
+        oc.init(cm);
+        const bool int_rep = opt.int_rep > 0 && detect_interior && !oc.trap;
         double sdzr = 1e300, sdzi = 1e300;
         int sk = -1, save_j2 = j, twin2 = 1;
         bool fin = false;
@@ -1907,7 +1989,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                     twin2 += twin2;
                 }
             }
-            if (use_bla && dzr * dzr + dzi * dzi < bla_rmax2) {
+            if (use_bla && !oc.trap && dzr * dzr + dzi * dzi < bla_rmax2) { // mp.cpp:2121
                 int skip = tryBLA(rkm1, dzr, dzi, ddr, ddi, dcr, dci, deriv, mx_ref_it);
                 if (skip > 0) {
                     ++blas;
@@ -1917,6 +1999,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                     rk += skip;
                     if (per && rk >= per) rk -= per;
                     rkm1 = (per && rk == 0) ? per - 1 : rk - 1;
+                    oc.skipped(); // mp.cpp:2422-2427
                     zsr = 1e30;
                     zsi = 1e30;
                     save_j = j;
@@ -1952,6 +2035,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
             zr = dzr + zfr[rk];
             zi = dzi + zfi[rk];
             zrad = zr * zr + zi * zi;
+            oc.push(zr, zi); // mp.cpp:2471-2472
             ++k;
             rkm1 = rk;
             if (per) {
@@ -1967,6 +2051,8 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                 } else if (de_ovl) {
                     setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
                     if (normal_) normal_[idx(arr)] = (float)(std::sqrt(zrad) / dxf * std::log(zrad) / std::sqrt(dr * dr + di * di));
+                } else if (oc.sac || oc.trap) { // mp.cpp:2497-2500
+                    setPixel(arr, oc.escaped(j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), (double)zrad, (double)escf), j + 1);
                 } else {
                     setPixel(arr, j + 1 - std::log(std::log((double)zrad) / 2 / std::log(2)) / std::log(2), j + 1);
                 }
@@ -1983,7 +2069,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
                         bool ret = (pr * pr + pi * pi < interior_eps2 * zrad);
                         if (ret && conf_D2 < 1.0) {
                             if (++conf_count >= interior_confirm) {
-                                setPixel(arr, -2, -1);
+                                setPixel(arr, oc.interior(), -1);
                                 done[i] = 1;
                                 fin = true;
                                 break;
@@ -2041,7 +2127,7 @@ void Engine::stepParallel(std::set<std::array<int, 4>>& s, int mx_ref_it, int mx
         }
         (void)fin;
         if (j >= mxit) {
-            setPixel(arr, -2, -1);
+            setPixel(arr, oc.interior(), -1);
             done[i] = 1;
         }
     }
@@ -2160,6 +2246,10 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
                     iter_[idx(p)] = (float)floatPoint(c0r + dxf * j, cim, mxit, cm, &nv, &nn);
                     if (escn_) escn_[idx(p)] = nn;
                     if (normal_) normal_[idx(p)] = (float)nv;
+                } else if (cm & (CM_SAC | CM_TRAP)) { // scalar path (mp.cpp:1459, 1512-1515)
+                    iter_[idx(p)] = (float)floatPoint(c0r + dxf * j, cim, mxit, cm, nullptr, &nn);
+                    if (ede && iter_[idx(p)] >= 0) iter_[idx(p)] /= dxf;
+                    if (escn_) escn_[idx(p)] = nn;
                 } else if (!deovl) {
                     double val = shallowSimd(c0r + dxf * j, cim, mxit, cm, &nn);
                     if (ede && val >= 0) val /= dxf;

@@ -42,12 +42,17 @@ def main():
     if not build_oracle.build_reference():
         raise SystemExit("reference sources / x86 toolchain unavailable")
     cases = json.load(open(os.path.join(HERE, "cases.json")))
+    only = sys.argv[sys.argv.index("--cases") + 1].split(",") if "--cases" in sys.argv else None
     for name, c in cases.items():
+        if only is not None and name not in only:
+            continue
         env = dict(os.environ, MANDEL_BAILOUT=repr(float(c["bailout"])), MANDEL_COARSE="0", OMP_NUM_THREADS=str(os.cpu_count()))
         out = os.path.join(HERE, "ref_%s.f32" % name)
         cmd = [DUMP, c["center_re"], c["center_im"], c["scale"], str(c["width"]), str(c["height"]), str(c["max_iterations"]), str(c["sub"]), str(c["coloring_method"]), out]
         subprocess.check_call(cmd, env=env, stdout=subprocess.DEVNULL)
         print("wrote", out)
+    if only is not None:
+        return
     jcases = json.load(open(os.path.join(HERE, "julia_cases.json")))
     for name, c in jcases.items():
         env = dict(os.environ, MANDEL_BAILOUT=repr(float(c["bailout"])), OMP_NUM_THREADS=str(os.cpu_count()))

@@ -100,7 +100,7 @@ def test_device_outputs(backend):
 
 def test_invalid_requests_rejected(backend):
     c = CASES["c1"]
-    for bad in (dict(sub=2), dict(width=1), dict(max_iterations=0), dict(coloring_method=8), dict(row_base=5)):
+    for bad in (dict(sub=2), dict(width=1), dict(max_iterations=0), dict(coloring_method=128), dict(coloring_method=8 | 1, sub=3), dict(row_base=5)):
         kw = dict(sub=1)
         kw.update(bad)
         req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], kw.pop("width", 16), 9, kw.pop("max_iterations", 100), **kw)
@@ -123,3 +123,19 @@ def test_strip_render_matches_oracle_strips(backend):
         oit, _, oen, _ = oracle.render(c["center_re"], c["center_im"], c["scale"], c["width"], h, c["max_iterations"], bailout=c["bailout"], full_height=c["height"], row_base=base)
         assert_same(req.iterations, req.escape_iteration, oit, oen, "strip %d" % base)
         np.testing.assert_allclose(req.iterations.reshape(h, c["width"]), full[base : base + h], rtol=1e-5)
+
+
+def test_orbit_colourings_take_the_exact_form(backend):
+    """The stripe average and the orbit traps need every iteration's z in FP64:
+    a mixed-form request renders them in the exact form (identical outputs),
+    and they are refused with supersampling (their adaptive-SS criteria are
+    not built)."""
+    for name in ("exterior1000_sac", "minibrot875_trap", "c1_sac"):
+        c = CASES[name]
+        it, _, en, _ = gpu_render(backend, c)
+        mit, _, men, _ = gpu_render(backend, c, precision_mode=mbx.PRECISION_MIXED)
+        assert np.array_equal(it.view(np.uint32), mit.view(np.uint32)) and np.array_equal(en, men), name
+    c = CASES["shallow_sac"]
+    req = mbx.ComputeRequest(c["center_re"], c["center_im"], c["scale"], c["width"], c["height"], c["max_iterations"], sub=3,
+                             coloring_method=c["coloring_method"] | 1, bailout=c["bailout"])
+    assert backend.compute_status(req) == mbx.E_INVALID
