@@ -551,7 +551,7 @@ def main():
                "natural": c4_nat, "untrained_model": c4_un, "trained_model": c4_tr, "unit": UNIT,
                "identical_outputs": all(np.array_equal(a, b) and np.array_equal(a, c) for a, b, c in zip(c4_o0, c4_o1, c4_o2)),
                "full_image_s_at_trained_rate": c4_tr["ms_per_batch"] / 1e3 * (views.C4_W * views.C4_H) / c4_samples,
-               "model": "order_model_params.npz (trained offline on C1/C2 maps by order_train.py), 32 Adam steps on the batch"}
+               "model": "order_model_params.npz (trained offline by order_train.py on the maps of the 1280x720 1e-30 view and the three benchmark frames), 32 Adam steps on the batch"}
 
     # plain FP64 GPU form on a sample of the same views, and accuracy vs it
     if args.plain_sample == "full":
@@ -631,7 +631,7 @@ def main():
             "dtype": "f32 (floatexp; f64 decisions)",
             "data": "synthetic",
             "config": {
-                "workload": "1080p deep frames: C2's two (half-width 1e-300 and 1e-1000 at 1e-(k+5) from the period-14164 nucleus) and a 1e-1000 frame holding a whole period-1331 minibrot; maxiter 1e6, bailout 2^8",
+                "workload": "1080p deep frames: the precision frames (half-width 1e-300 and 1e-1000 at 1e-(k+5) from the period-14164 nucleus) and a 1e-1000 frame holding a whole period-1331 minibrot; maxiter 1e6, bailout 2^8",
                 "frames_per_step": len(vlist),
                 "resolution": "%dx%d" % (W, H),
                 "l2": "inputs (orbit, BLA table) L2/smem resident by design; outputs 2x 8.3 MB written per frame; no flush",

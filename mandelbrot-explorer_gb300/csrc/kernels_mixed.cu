@@ -640,8 +640,8 @@ cudaError_t launch_batch_pass(int tier, const BatchArgs& a, int nsm, cudaStream_
             k_batch_pass<df32, 128, 2, 32, true><<<nsm * 4, 128, 0, st>>>(b);
         } else {
             // 128 registers without spills: four blocks of 128 per SM (a
-            // batch's queue holds many waves of samples; measured on 24 C4
-            // tiles, 1.2M queued: 372 -> 332 ms)
+            // batch's queue holds many waves of samples; measured on 24
+            // tiles of the 1e-500 image, 1.2M queued: 372 -> 332 ms)
             k_batch_pass<df32, 128, 4, 8><<<nsm * 4, 128, 0, st>>>(b);
             k_batch_pass<df32, 128, 4, 32><<<nsm * 4, 128, 0, st>>>(b);
         }

@@ -151,7 +151,8 @@ def c3_views(seed: int = 3, n: int = 64, size_div: int = 1):
 # views_data.json ("c4", size 3.2e-501: the minibrot spans about a third of
 # the view's width; it is the copy of the standard set's period-5 real-axis
 # minibrot inside a period-7609
-# minibrot found by a seeded search next to the C2 nucleus). The view is
+# minibrot found by a seeded search next to the period-14164 nucleus of the
+# deep frames). The view is
 # centred 1e-3 of the view width outward from a point of that minibrot's edge:
 # the boundary pixel nearest a seed-drawn point of the estimated main cardioid
 # (nucleus + size (e/2 - e^2/4)), refined by renders at shrinking half-widths
@@ -176,7 +177,7 @@ def c4_cardioid_point(seed: int = 4):
 
 
 def c4_view():
-    """Centre, half-width and pitch of the whole C4 image (decimals)."""
+    """Centre, half-width and pitch of the whole learned-scheduling image (decimals)."""
     d = nucleus()["c4"]
     getcontext().prec = len(d["nucleus_re"]) + 20
     hw = Decimal(10) ** C4_HW_LOG10
@@ -188,7 +189,7 @@ def c4_view():
 
 
 def c4_edge_search(be, seed: int = 4, n: int = 512, levels: int = 8):
-    """The boundary of the C4 minibrot near its seed-drawn cardioid point:
+    """The boundary of the learned-scheduling image's minibrot near its seed-drawn cardioid point:
     render n x n at maxiter 2e6 around the current point, take the boundary
     pixel (non-escaping, with an escaping 4-neighbour) nearest it, divide the
     half-width by 32, repeat down to a half-width below 1e-502. Returns the
@@ -240,9 +241,9 @@ def c4_edge_search(be, seed: int = 4, n: int = 512, levels: int = 8):
 
 
 def c4_tiles(seed: int = 4, n: int = 32, tile: int = 256):
-    """n seed-drawn tile x tile tiles of the C4 image (without repeats), each a
+    """n seed-drawn tile x tile tiles of the learned-scheduling image (without repeats), each a
     view with the image's pixel pitch, its centre at the tile's centre. Every
-    tile names the C4 nucleus as its periodic reference (one orbit for all)."""
+    tile names the image's minibrot nucleus as its periodic reference (one orbit for all)."""
     v = c4_view()
     d = nucleus()["c4"]
     getcontext().prec = len(d["nucleus_re"]) + 20

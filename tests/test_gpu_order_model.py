@@ -3,15 +3,16 @@
 * gradient check: the summed gradients of the tensor-core training kernels
   (tcgen05, minibatch rows spread over blocks) against the CPU reference
   (tests/order_ref.py) of the same BF16 MLP, over 256 and 384 rows;
-* the learned-scheduling workload (C4): 24 seed-drawn 256x256 tiles of the
+* the learned-scheduling workload: 24 seed-drawn 256x256 tiles of the
   23040x12960 image (half-width 1e-500 at a minibrot's edge, maxiter 2e6) as
   one batch. The ordering changes no output (identical to the natural order in
   every mode), and the main FP32 pass that it orders is faster with the model
   than in the natural order (measured 81 -> 52.6 ms) and than with the
   untrained model, whose prediction is the tiles' mean probe cost (53.3 ms,
   min of two; three repeats of each differed by 0.1 ms): the trained model is
-  the committed one (trained offline on the C1/C2 iteration maps by
-  order_train.py), trained further on this batch's own map.
+  the committed one (trained offline by order_train.py on the iteration maps
+  of the 1e-30 view and the 1080p benchmark frames), trained further on this
+  batch's own map.
 """
 import numpy as np
 import pytest
@@ -85,7 +86,7 @@ def test_learned_order_on_c4_tiles():
         out, tr_f32, tr_graph = _run(be, tiles)
         for (it, en), (bit, ben) in zip(out, base):
             assert np.array_equal(en, ben) and np.array_equal(it, bit)
-        print("\n[order C4 x24] FP32 pass: natural %.2f, untrained %.2f, trained %.2f ms; shared passes: %.1f, %.1f, %.1f ms"
+        print("\n[order 1e-500 tiles x24] FP32 pass: natural %.2f, untrained %.2f, trained %.2f ms; shared passes: %.1f, %.1f, %.1f ms"
               % (nat_f32, un_f32, tr_f32, nat_graph, un_graph, tr_graph))
         assert tr_f32 < 0.8 * nat_f32
         assert tr_f32 < un_f32
