@@ -357,7 +357,7 @@ def main():
     torch.cuda.synchronize()
     b_elapsed = time.perf_counter() - t0
     batched = {"ms_per_step": b_elapsed / args.steps * 1e3, "value": b_eff / b_elapsed / 1e9, "unit": UNIT, "shared_passes_gpu_ms": b_gpu / args.steps,
-               "note": "mbx_compute_batch: one CUDA graph per step holding the frames' probe, main and rerun passes; default launch shape"}
+               "note": "mbx_compute_batch: frames of 2^20 pixels or more (these three) render on their own streams as soon as their host work is done; smaller frames share one CUDA graph of probe, main and rerun passes; default launch shape"}
     # the learned-scheduled form: the cost model trains on the warm-up batches
     # (mode 1), then orders the timed ones (mode 2); outputs are identical
     ref_out = [o[1].clone() for o in outs]

@@ -181,9 +181,12 @@ int mbx_find_nucleus(const char* center_re, const char* center_im, const char* r
  * and replayed while the batch keeps its shape; what no lane tier vouches for
  * is finished per frame in the exact form, and the adaptive-supersampling
  * passes of supersampled frames run per frame after the graph, on the frames'
- * own streams from concurrent host threads. Other frames (shallow, exact
- * form, and supersampled frames while the learned ordering is on) are rendered
- * one by one. Results are identical to mbx_compute of each frame. view_stats
+ * own streams from concurrent host threads. Frames of 2^20 pixels or more
+ * (mbx_set_batch_direct; unless the learned ordering is on) and other frames (shallow, exact form,
+ * orbit colourings, and supersampled frames while the learned ordering is on)
+ * are rendered on their own, each on its engine's stream from the host thread
+ * that prepared it, so a large frame's passes overlap the other frames' host
+ * work. Results are identical to mbx_compute of each frame. view_stats
  * (n entries) and batch_stats may be NULL; the shared passes' counters go to
  * batch_stats. Frames need fewer than 65536 sample rows. */
 int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_stats* batch_stats);
@@ -200,6 +203,12 @@ int mbx_compute_batch(mbx_context* ctx, const mbx_request* reqs, int n, mbx_stat
  * predicts a tile's mean probe cost. Outputs are identical in every mode.
  * 0 (default): natural order. */
 int mbx_set_batch_scheduling(mbx_context* ctx, int mode);
+
+/* Frames of mbx_compute_batch with at least `pixels` pixels (default 2^20)
+ * render on their own as soon as their host work is done instead of joining
+ * the shared graph; pixels <= 0 keeps every eligible frame in the graph.
+ * Results are identical either way. */
+int mbx_set_batch_direct(mbx_context* ctx, long long pixels);
 
 /* Diagnostics of the ordering model: parameters (5825 floats: W1 [64][24], b1
  * [64], W2 [64][64], b2 [64], w3 [64], b3) set and/or read, and the gradients

@@ -311,11 +311,26 @@ int BatchRunner::run(const mbx_request* reqs, int n, mbx_stats* view_stats, mbx_
         // independent per engine: up to `lanes` engines build concurrently,
         // each thread with its own product helpers (up to seven threads each
         // while a loop runs), so the lane count follows the host's cores.
+        // A frame of at least direct_pixels_ pixels fills the GPU by itself:
+        // unless the learned ordering wants every frame in the shared graph,
+        // it renders on its own engine's stream as soon as its host work is
+        // done, overlapping the other frames' host work (its thread then
+        // mostly waits on the stream, hence up to one more lane).
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        const int lanes = std::max(1, std::min({n, 4, (int)(hw / 7)}));
+        int direct = 0;
+        std::vector<char> is_direct((size_t)n, 0);
+        for (int i = 0; i < n; ++i) {
+            const long long px = (long long)reqs[i].width * reqs[i].height;
+            if (schedule_ == 0 && direct_pixels_ > 0 && px >= direct_pixels_) {
+                is_direct[(size_t)i] = 1;
+                ++direct;
+            }
+        }
+        const int lanes = std::max(1, std::min({n, 4, (int)(hw / 7) + (direct ? 1 : 0)}));
         std::vector<int> rcs((size_t)n, MBX_OK);
         auto work = [&](int t) {
-            for (int i = t; i < n; i += lanes) rcs[(size_t)i] = eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
+            for (int i = t; i < n; i += lanes)
+                rcs[(size_t)i] = is_direct[(size_t)i] ? eng_[i]->compute(reqs[i], &vst[i]) : eng_[i]->compute_deferred(reqs[i], &slots[i], &vst[i]);
         };
         std::vector<std::thread> th;
         for (int t = 1; t < lanes; ++t) th.emplace_back(work, t);

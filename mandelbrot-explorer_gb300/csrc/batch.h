@@ -13,6 +13,9 @@
 
 namespace mbx {
 
+// default: frames of at least this many pixels render on their own, not in the shared graph
+constexpr long long kBatchDirectSamples = 1ll << 20;
+
 class BatchRunner {
   public:
     explicit BatchRunner(int device) : device_(device) {}
@@ -25,6 +28,7 @@ class BatchRunner {
     // 1: order each batch's main pass by the learned cost model and train it on
     // the batch's costs; 2: order with the model as it stands; 0: natural order
     int set_schedule(int mode, std::string& err);
+    void set_direct(long long pixels) { direct_pixels_ = pixels; }
     int schedule_params(const float* set, float* get, std::string& err);
     int schedule_gradient(const float* features, const float* targets, int n, float* grad, std::string& err);
 
@@ -58,6 +62,7 @@ class BatchRunner {
     int g_deriv_ = -1;     // the captured graph's lanes carry the derivative (DE colourings)
     // learned ordering
     int schedule_ = 0;
+    long long direct_pixels_ = kBatchDirectSamples; // <= 0: every frame joins the shared graph
     SchedState sched_{};
     bool sched_ready_ = false;
     uint64_t* d_qo_ = nullptr;       // the main FP32 pass's order (sample indices), then the double-float queue

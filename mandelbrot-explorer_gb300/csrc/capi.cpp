@@ -156,6 +156,16 @@ int mbx_set_batch_scheduling(mbx_context* c, int mode) {
     return rc;
 }
 
+int mbx_set_batch_direct(mbx_context* c, long long pixels) {
+    if (!c) return MBX_E_INVALID;
+    std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);
+    if (!busy.owns_lock()) return MBX_E_BUSY;
+    mbx::BatchRunner* b = batch_of(c);
+    if (!b) return MBX_E_NOMEM;
+    b->set_direct(pixels);
+    return MBX_OK;
+}
+
 int mbx_schedule_params(mbx_context* c, const float* set, float* get) {
     if (!c || (!set && !get)) return MBX_E_INVALID;
     std::unique_lock<std::mutex> busy(c->mu, std::try_to_lock);

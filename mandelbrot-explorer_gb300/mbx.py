@@ -149,6 +149,7 @@ EXPORTS = (
     "mbx_autotune",
     "mbx_compute_batch",
     "mbx_set_batch_scheduling",
+    "mbx_set_batch_direct",
     "mbx_schedule_params",
     "mbx_schedule_gradient",
     "mbx_color_defaults",
@@ -228,6 +229,8 @@ def load_library(path: Optional[str] = None, build_if_missing: bool = True):
         lib.mbx_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Request), ctypes.POINTER(Tuning)]
         lib.mbx_set_batch_scheduling.restype = ctypes.c_int
         lib.mbx_set_batch_scheduling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.mbx_set_batch_direct.restype = ctypes.c_int
+        lib.mbx_set_batch_direct.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
         lib.mbx_schedule_params.restype = ctypes.c_int
         lib.mbx_schedule_params.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.mbx_schedule_gradient.restype = ctypes.c_int
@@ -452,6 +455,10 @@ class CudaComputeBackend:
     def set_batch_scheduling(self, mode: int) -> int:
         """Learned ordering of the batched main pass: 1 on, 0 off."""
         return self._lib.mbx_set_batch_scheduling(self._ctx, int(mode))
+
+    def set_batch_direct(self, pixels: int) -> int:
+        """Batch frames of at least `pixels` pixels render on their own (<= 0: never)."""
+        return self._lib.mbx_set_batch_direct(self._ctx, int(pixels))
 
     def schedule_params(self, set_params=None) -> np.ndarray:
         """Reads (and first sets, when given) the ordering model's parameters."""

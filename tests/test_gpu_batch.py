@@ -78,6 +78,7 @@ def test_batch_exact_form_leftovers_match_single_frames():
     form after its graph, as mbx_compute does after its tiers: same samples,
     same values."""
     be = mbx.create_compute_backend("cuda")
+    assert be.set_batch_direct(0) == mbx.OK  # the 1080p frame joins the shared graph
     frames = [(views.deep_view(300), 1920, 1080), (views.deep_view(1000), 160, 90)]
     singles = []
     for v, w, h in frames:
@@ -95,3 +96,27 @@ def test_batch_exact_form_leftovers_match_single_frames():
         assert np.array_equal(r.escape_iteration, en) and np.array_equal(r.iterations, it)
     print("\n[batch] exact-form leftovers: %d" % bs["exact_reruns"])
     be.close()
+
+
+def test_large_frames_render_directly_and_identically():
+    """Frames of 2^20 pixels or more render on their own streams as soon as
+    their host work is done (overlapping the others'), the rest in the shared
+    graph; outputs are those of one-frame renders."""
+    frames = [(views.deep_view(300), 1280, 820), (views.minibrot_view(), 1024, 1024), (views.deep_view(1000), 160, 90)]
+    be = mbx.create_compute_backend("cuda")
+    try:
+        singles = []
+        for v, w, h in frames:
+            r = _req(v, w, h)
+            assert be.compute_status(r) == mbx.OK, be.last_error()
+            singles.append((r.iterations.copy(), r.escape_iteration.copy()))
+        reqs = [_req(v, w, h) for v, w, h in frames]
+        assert be.compute_batch(reqs) == mbx.OK, be.last_error()
+        bs = be.last_batch_stats.as_dict()
+        # only the small frame's probe and main samples went through the shared graph
+        assert bs["samples"] < 2 * 160 * 90
+        for (it, en), r, (v, w, h) in zip(singles, reqs, frames):
+            assert np.array_equal(r.escape_iteration, en), (w, h)
+            assert np.array_equal(r.iterations, it), (w, h)
+    finally:
+        be.close()
