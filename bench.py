@@ -283,7 +283,7 @@ def main():
     outs = [(torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.int32, device="cuda")) for _ in vlist]
     reruns = {}
 
-    per_frame = {v["label"]: dict(eff=0, steps=0, bla=0, gpu_ms=0.0, fp32_ms=0.0, fp32_steps=0, fp32_bla=0) for v in vlist}
+    per_frame = {v["label"]: dict(eff=0, steps=0, bla=0, gpu_ms=0.0, fp32_ms=0.0, fp32_steps=0, fp32_bla=0, rerun_ms=0.0, exact_ms=0.0) for v in vlist}
 
     def step(reuse=True, record=False):
         eff = steps = bla = launches = 0
@@ -308,6 +308,8 @@ def main():
                 pf["fp32_ms"] += st["fp32_pass_gpu_ms"]
                 pf["fp32_steps"] += st["fp32_pass_steps"]
                 pf["fp32_bla"] += st["fp32_pass_bla_applies"]
+                pf["rerun_ms"] += st["rerun_gpu_ms"]
+                pf["exact_ms"] += st["rerun_fp64_gpu_ms"]
         return eff, steps, bla, launches, gpu_ms, per_view
 
     # warm-up (the first step builds each frame's reference)
@@ -590,6 +592,9 @@ def main():
             "gpixel_iter_per_s": pf["eff"] / sec / 1e9 if sec > 0 else None,
             "executed_steps_per_s": pf["steps"] / sec if sec > 0 else None,
             "bla_applies_per_s": pf["bla"] / sec if sec > 0 else None,
+            # device time of the tiers (CUDA events): FP32 lanes, double-float lanes, exact form
+            "tier_gpu_ms": {"fp32": pf["fp32_ms"] / args.steps, "double_float": (pf["rerun_ms"] - pf["exact_ms"]) / args.steps,
+                            "exact_form": pf["exact_ms"] / args.steps},
             "fp32_pass": {"gpu_ms": pf["fp32_ms"] / args.steps, "steps": pf["fp32_steps"] // args.steps, "bla_applies": pf["fp32_bla"] // args.steps,
                           "tflops": (FLOPS_PER_STEP * pf["fp32_steps"] + FLOPS_PER_BLA * pf["fp32_bla"]) / (pf["fp32_ms"] / 1e3) / 1e12 if pf["fp32_ms"] > 0 else None},
         }
@@ -609,6 +614,14 @@ def main():
         ext = (tn > 0) & (en > 0)
         truth_acc[v["label"]] = {"samples": int(idx.numel()), "escape_iteration_identical": float(np.mean(en == tn)), "class_mismatch": int(np.sum((en < 0) != (tn < 0))),
                                  "max_abs_dmu": float(np.max(np.abs(mu[ext] - tv[ext]), initial=0.0))}
+
+    # share of the step's device time per tier (all frames)
+    tot_tier = {"fp32": 0.0, "double_float": 0.0, "exact_form": 0.0}
+    for f_ in frames.values():
+        for k_, x_ in f_["tier_gpu_ms"].items():
+            tot_tier[k_] += x_
+    s_ = sum(tot_tier.values()) or 1.0
+    tier_share = {k_: {"gpu_ms": x_, "share": x_ / s_} for k_, x_ in tot_tier.items()}
 
     cpu = None
     if rank == 0:
@@ -661,7 +674,9 @@ def main():
                          "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                          "algorithmic": "25 flops per executed delta step + 19 per BLA application (mp.cpp:2457-2469, 2558, 2732-2740), over the kernel's CUDA-event time",
                          "all_passes": {"achieved": achieved_all, "frac": achieved_all / fp32_peak if fp32_peak else None, "note": "every delta pass of the frames (FP32, double-float and exact-form tiers) over their GPU time"},
-                         "peak_source": "measured in-run FMA issue rate (mbx_measure_fma_peak); MEASURED_PEAKS.json holds only HBM and bf16", "fp64_peak": fp64_peak},
+                         "peak_source": "measured in-run FMA issue rate (mbx_measure_fma_peak); MEASURED_PEAKS.json holds only HBM and bf16", "fp64_peak": fp64_peak,
+                         "step_time_by_tier": tier_share,
+                         "note_largest": "by device time the double-float tier (k_lane_pass<df32>) is the step's largest kernel, on the minibrot frame: latency-bound chains of the longest samples (profiles/k_lane_pass_df32_minibrot1000_1080p_ncu.md), far below any throughput roof; the FP32 lane is reported as the roofline kernel because it carries the step's arithmetic"},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": tot[3],
