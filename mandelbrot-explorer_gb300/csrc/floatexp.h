@@ -38,6 +38,38 @@ MBX_HD double bitsd(uint64_t b) {
 }
 MBX_HD double dabs(double x) { return bitsd(dbits(x) & 0x7fffffffffffffffull); }
 
+// Comparisons on the bit patterns, with exactly the IEEE results (NaN
+// included): integer compares, where an FP64 compare costs the latency of an
+// FP64 add (64 cycles on GB300, against 4 for an FP32 FMA).
+// x == 0.0 (either sign)
+MBX_HD bool d_is_zero(double x) { return (dbits(x) << 1) == 0; }
+// |a| < |b|; for a and b +0, positive or NaN (a sum of squares, a squared
+// radius) this is a < b
+MBX_HD bool d_abs_less(double a, double b) {
+    const uint64_t ua = dbits(a) & 0x7fffffffffffffffull, ub = dbits(b) & 0x7fffffffffffffffull;
+    return ua < ub && ub <= 0x7ff0000000000000ull;
+}
+// a == b (+0 equals -0, NaN equals nothing)
+MBX_HD bool d_eq(double a, double b) {
+    const uint64_t ua = dbits(a), ub = dbits(b);
+    return (ua == ub && (ua & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull) || ((ua | ub) << 1) == 0;
+}
+// x <= 0.0
+MBX_HD bool d_le_zero(double x) {
+    const uint64_t u = dbits(x);
+    return (u << 1) == 0 || ((u >> 63) != 0 && (u & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull);
+}
+// x + x, exactly as the FP64 add rounds it, on the bit pattern for finite x
+MBX_HD double d_twice(double x) {
+    const uint64_t b = dbits(x);
+    const uint64_t e = (b >> 52) & 0x7ff;
+    if (e - 1 < 0x7fd) return bitsd(b + (1ull << 52)); // normal, result normal
+    if (e == 0) // zero or subnormal: the magnitude shifts (a carry into the exponent gives the normal result)
+        return bitsd((b & 0x8000000000000000ull) | ((b & 0x7fffffffffffffffull) << 1));
+    if (e == 0x7fe) return bitsd((b & 0x8000000000000000ull) | 0x7ff0000000000000ull); // overflows to infinity
+    return x + x; // infinity, NaN
+}
+
 // frexp: x = r * 2^e with 0.5 <= |r| < 1; zero, inf and nan return x with e = 0.
 MBX_HD double xfrexp(double x, int* e) {
     uint64_t b = dbits(x);
@@ -68,7 +100,7 @@ MBX_HD double pow2i(int k) {
 
 // ldexp for finite x, correctly rounded (one rounding in the subnormal range).
 MBX_HD double xldexp(double x, int k) {
-    if (x == 0.0) return x;
+    if (d_is_zero(x)) return x;
     uint64_t b = dbits(x);
     if (((b >> 52) & 0x7ff) == 0x7ff) return x;
     int e;
@@ -96,35 +128,35 @@ MBX_HD FE fe_make(double m, int64_t e) {
     return r;
 }
 MBX_HD FE fe_from(double x) {
-    if (x == 0.0) return fe_make(0.0, 0);
+    if (d_is_zero(x)) return fe_make(0.0, 0);
     int ex;
     double mm = xfrexp(x, &ex);
     return fe_make(mm, (int64_t)ex);
 }
 MBX_HD double fe_to_double(FE a) {
-    if (a.m == 0.0) return 0.0;
+    if (d_is_zero(a.m)) return 0.0;
     if (a.e > 1100) return bitsd(a.m > 0 ? 0x7ff0000000000000ull : 0xfff0000000000000ull);
     if (a.e < -1100) return 0.0;
     return xldexp(a.m, (int)a.e);
 }
 MBX_HD FE fe_renorm(double m, int64_t e) {
-    if (m == 0.0) return fe_make(0.0, 0);
+    if (d_is_zero(m)) return fe_make(0.0, 0);
     int ex;
     double mm = xfrexp(m, &ex);
     return fe_make(mm, e + ex);
 }
 MBX_HD FE fe_mul(FE a, FE b) {
-    if (a.m == 0.0 || b.m == 0.0) return fe_make(0.0, 0);
+    if (d_is_zero(a.m) || d_is_zero(b.m)) return fe_make(0.0, 0);
     return fe_renorm(a.m * b.m, a.e + b.e);
 }
 MBX_HD FE fe_mul_d(FE a, double b) {
-    if (a.m == 0.0 || b == 0.0) return fe_make(0.0, 0);
+    if (d_is_zero(a.m) || d_is_zero(b)) return fe_make(0.0, 0);
     return fe_renorm(a.m * b, a.e);
 }
-MBX_HD FE fe_scale2(FE a, int64_t k) { return a.m == 0.0 ? a : fe_make(a.m, a.e + k); }
+MBX_HD FE fe_scale2(FE a, int64_t k) { return d_is_zero(a.m) ? a : fe_make(a.m, a.e + k); }
 MBX_HD FE fe_add(FE a, FE b) {
-    if (a.m == 0.0) return b;
-    if (b.m == 0.0) return a;
+    if (d_is_zero(a.m)) return b;
+    if (d_is_zero(b.m)) return a;
     int64_t d = a.e - b.e;
     if (d > 54) return a;
     if (d < -54) return b;
@@ -134,14 +166,14 @@ MBX_HD FE fe_add(FE a, FE b) {
 MBX_HD FE fe_neg(FE a) { return fe_make(-a.m, a.e); }
 MBX_HD FE fe_sub(FE a, FE b) { return fe_add(a, fe_neg(b)); }
 MBX_HD FE fe_div(FE a, FE b) {
-    if (a.m == 0.0) return fe_make(0.0, 0);
+    if (d_is_zero(a.m)) return fe_make(0.0, 0);
     return fe_renorm(a.m / b.m, a.e - b.e);
 }
 MBX_HD bool fe_abs_less(FE a, FE b) {
-    if (a.m == 0.0) return b.m != 0.0;
-    if (b.m == 0.0) return false;
+    if (d_is_zero(a.m)) return !d_is_zero(b.m);
+    if (d_is_zero(b.m)) return false;
     if (a.e != b.e) return a.e < b.e;
-    return dabs(a.m) < dabs(b.m);
+    return d_abs_less(a.m, b.m);
 }
 MBX_HD double xsqrt(double x) {
 #ifdef __CUDA_ARCH__

@@ -389,19 +389,23 @@ __device__ void fe_deriv_underflow(FE zr, FE zi, FE& SJ, double& jr, double& ji,
 }
 
 // tryBLAfe (mp.cpp:2883-2970).
-__device__ int bla_try_fe(const BlaView& b, const double2* Z, bool periodic, int s, FE& S, FE S2, double& wr, double& wi, double dr, double di, double ESC2, int mx_ref_it, double* ab) {
+// wm2: wr * wr + wi * wi when the caller has it (else a negative value)
+__device__ int bla_try_fe(const BlaView& b, const double2* Z, bool periodic, int s, FE& S, FE S2, double& wr, double& wi, double dr, double di, double ESC2, int mx_ref_it, double* ab,
+                          double wm2 = -1.0) {
     if (s < 1 || b.nlev == 0) return 0;
     int maxp = b.nlev - 1;
     int startp = (s == 1) ? maxp : __ffs(s - 1) - 1;
     if (startp > maxp) startp = maxp;
     if (startp < b.minlevel) return 0;
-    FE dz2 = fe_mul(S2, fe_from(wr * wr + wi * wi));
+    double w2 = wm2;
+    if (dbits(wm2) >> 63) w2 = wr * wr + wi * wi; // (not known)
+    FE dz2 = fe_mul(S2, fe_from(w2));
     if (b.rmax2 <= 0.0 || !fe_abs_less(dz2, fe_from(b.rmax2))) return 0;
     for (int p = startp; p >= b.minlevel; --p) {
         int i = (s - 1) >> p;
         if (i >= b.size[p]) continue;
         double r2 = b.r2[b.off[p] + i];
-        if (r2 <= 0 || !fe_abs_less(dz2, fe_from(r2))) continue;
+        if (d_le_zero(r2) || !fe_abs_less(dz2, fe_from(r2))) continue;
         int l = 1 << p;
         int land = s + l;
         if (land >= mx_ref_it - 1) continue;
@@ -410,12 +414,12 @@ __device__ int bla_try_fe(const BlaView& b, const double2* Z, bool periodic, int
         double nwi = (bc.x * wi + bc.y * wr) + (bc.z * di + bc.w * dr);
         const double BIG = 1e150;
         double2 zl = Z[land];
-        if (isfinite(nwr) && isfinite(nwi) && dabs(nwr) < BIG && dabs(nwi) < BIG) {
+        if (d_abs_less(nwr, BIG) && d_abs_less(nwi, BIG)) { // (finite, below 1e150)
             double fr = zl.x + fe_to_double(fe_mul_d(S, nwr));
             double fi = zl.y + fe_to_double(fe_mul_d(S, nwi));
-            if (fr * fr + fi * fi > ESC2) return 0;
+            if (d_abs_less(ESC2, fr * fr + fi * fi)) return 0; // > ESC2
             double wm2 = nwr * nwr + nwi * nwi;
-            if (wm2 == 0.0) {
+            if (d_is_zero(wm2)) {
                 if (periodic)
                     bla_rerescale_underflow(S, wr, wi, nwr, nwi);
                 else
@@ -462,6 +466,29 @@ struct PixOut {
     int state; // 1 escaped, 2 interior, 4 cancelled
 };
 
+// The plain delta step of pixelRescaled: w' = (2 X + s w) w + d in the fused
+// form, 2 (X w) + s w^2 + d otherwise. On GB300 each FP64 instruction holds
+// its SM quarter's FP64 unit for 64 cycles, independent operands or not, so
+// the exact form's loops are bound by their count of FP64 instructions: the
+// doubling X + X (exact) is formed on the bit pattern, and the tests below
+// compare bit patterns (floatexp.h d_is_zero, d_abs_less, d_eq), with the
+// IEEE results.
+__device__ __forceinline__ void fe_plain_step(bool fused, double Xr, double Xi, double s, double wr, double wi, double dr, double di, double& nwr, double& nwi) {
+    if (fused) {
+        const double fR = d_twice(Xr) + s * wr;
+        const double fI = d_twice(Xi) + s * wi;
+        nwr = fR * wr - fI * wi + dr;
+        nwi = fR * wi + fI * wr + di;
+    } else {
+        double w2r = wr * wr - wi * wi, w2i = 2.0 * wr * wi;
+        nwr = 2.0 * (Xr * wr - Xi * wi) + s * w2r + dr;
+        nwi = 2.0 * (Xr * wi + Xi * wr) + s * w2i + di;
+    }
+}
+// |x| < 2^-1056 (the subnormal 2^18 * 2^-1074): the step's underflow test, on
+// the bit pattern
+__device__ __forceinline__ bool below_step_floor(double x) { return (dbits(x) & 0x7fffffffffffffffull) < 0x40000ull; }
+
 // pixelRescaled (mp.cpp:3287-3618), smooth / EDE / DE-overlay.
 // OC: the orbit colourings, as in k_fp64_pass (mp.cpp:3338-3346, 3389-3397,
 // 3503-3504, 3524-3529); a trap turns BLA off.
@@ -505,13 +532,18 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
     o.nrm = 0.0f;
     o.n = -1;
     int tick = 0;
+    // |w|^2 of the current state when the previous iteration formed it (a
+    // step with no rescale or rebase after it), else -1
+    double wm2_known = -1.0;
     while (iter < g.mxit) {
+        const double wm2_now = wm2_known;
+        wm2_known = -1.0;
         if (((++tick) & 4095) == 0 && cancelled(f)) {
             o.state = 4;
             return o;
         }
         if (int_rep) {
-            if (m == sm && wr == swr && wi == swi && S.m == sS.m && S.e == sS.e) {
+            if (m == sm && d_eq(wr, swr) && d_eq(wi, swi) && d_eq(S.m, sS.m) && S.e == sS.e) {
                 o.value = -2.0f;
                 o.state = 2;
                 return o;
@@ -527,7 +559,7 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
         }
         if (f.bla.use && !(OC & kOcTrap) && m >= 2) {
             double ab[4];
-            int skip = bla_try_fe(f.bla, Z, p.ref_period_gt0, rm, S, S2, wr, wi, dr, di, g.ESC2, per ? per : reflen, deriv ? ab : nullptr);
+            int skip = bla_try_fe(f.bla, Z, p.ref_period_gt0, rm, S, S2, wr, wi, dr, di, g.ESC2, per ? per : reflen, deriv ? ab : nullptr, wm2_now);
             if (skip > 0) {
                 ++n_bla;
                 n_skip += skip;
@@ -567,8 +599,14 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
         ++n_steps;
         double2 X = m ? Z[rm] : make_double2(0.0, 0.0);
         double Xr = X.x, Xi = X.y;
-        double zmr = Xr + s * wr, zmi = Xi + s * wi;
-        const bool deriv_underflow = deriv && zmr == 0.0 && zmi == 0.0 && invSJd == 0.0;
+        // the pre-step z (DE colourings only)
+        double zmr = 0.0, zmi = 0.0;
+        bool deriv_underflow = false;
+        if (deriv) {
+            zmr = Xr + s * wr;
+            zmi = Xi + s * wi;
+            deriv_underflow = d_is_zero(zmr) && d_is_zero(zmi) && d_is_zero(invSJd);
+        }
         FE zmrfe = fe_make(0, 0), zmife = fe_make(0, 0);
         if (deriv_underflow) {
             FE Xrfe = m ? Zfe[rm].re : fe_make(0.0, 0);
@@ -577,18 +615,9 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
             zmife = fe_add(Xife, fe_mul_d(S, wi));
         }
         double nwr, nwi;
-        if (p.fused) {
-            const double fR = Xr + Xr + s * wr;
-            const double fI = Xi + Xi + s * wi;
-            nwr = fR * wr - fI * wi + dr;
-            nwi = fR * wi + fI * wr + di;
-        } else {
-            double w2r = wr * wr - wi * wi, w2i = 2.0 * wr * wi;
-            nwr = 2.0 * (Xr * wr - Xi * wi) + s * w2r + dr;
-            nwi = 2.0 * (Xr * wi + Xi * wr) + s * w2i + di;
-        }
-        const bool step_underflow = dabs(nwr) < 0x1p-1056 && dabs(nwi) < 0x1p-1056;
-        if (step_underflow && (nwr != 0.0 || nwi != 0.0 || wr != 0.0 || wi != 0.0 || dcr.m != 0.0 || dci.m != 0.0)) {
+        fe_plain_step(p.fused, Xr, Xi, s, wr, wi, dr, di, nwr, nwi);
+        const bool step_underflow = below_step_floor(nwr) && below_step_floor(nwi);
+        if (step_underflow && !(d_is_zero(nwr) && d_is_zero(nwi) && d_is_zero(wr) && d_is_zero(wi) && d_is_zero(dcr.m) && d_is_zero(dci.m))) {
             FE Xrfe = m ? Zfe[rm].re : fe_make(0.0, 0);
             FE Xife = m ? Zfe[rm].im : fe_make(0.0, 0);
             fe_step_underflow(Xrfe, Xife, dcr, dci, S, wr, wi);
@@ -628,8 +657,10 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
         Xi = X.y;
         double zr = Xr + s * wr, zi = Xi + s * wi;
         double zrad = zr * zr + zi * zi;
+        const double wmag2 = wr * wr + wi * wi;
+        bool keep = true;
         oc.push(zr, zi);
-        if (zrad > g.ESC2) {
+        if (d_abs_less(g.ESC2, zrad)) { // zrad > ESC2
             o.n = iter;
             o.state = 1;
             if (g.ede) {
@@ -655,10 +686,10 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
         if (detect) {
             if (conf_P > 0) {
                 conf_D2 *= 4.0 * zrad;
-                if (conf_D2 > 1e18) conf_D2 = 1e18;
+                if (d_abs_less(1e18, conf_D2)) conf_D2 = 1e18; // conf_D2 >= +0 or NaN
                 if (iter >= conf_next) {
                     double pr = zr - conf_zr, pi = zi - conf_zi;
-                    if (pr * pr + pi * pi < p.interior_eps2 * zrad && conf_D2 < 1.0) {
+                    if (d_abs_less(pr * pr + pi * pi, p.interior_eps2 * zrad) && d_abs_less(conf_D2, 1.0)) {
                         if (++conf_count >= p.interior_confirm) {
                             o.value = oc.interior();
                             o.state = 2;
@@ -675,7 +706,7 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 }
             } else if ((iter & 15) == 0 && conf_giveup < 3) {
                 double pr = zr - zsr, pi = zi - zsi;
-                if (pr * pr + pi * pi < p.interior_eps2 * zrad) {
+                if (d_abs_less(pr * pr + pi * pi, p.interior_eps2 * zrad)) {
                     conf_P = iter - save_iter;
                     if (conf_P < 1) conf_P = 1;
                     conf_zr = zr;
@@ -692,8 +723,8 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 }
             }
         }
-        double wmag2 = wr * wr + wi * wi;
-        if (wmag2 > 1e16 || (wmag2 < 1e-16 && wmag2 > 0.0)) {
+        // |w|^2 > 1e16, or 0 < |w|^2 < 1e-16 (|w|^2 >= +0 or NaN)
+        if (d_abs_less(1e16, wmag2) || (d_abs_less(wmag2, 1e-16) && !d_is_zero(wmag2))) {
             FE wmag = fe_sqrt(fe_from(wmag2));
             S = fe_mul(S, wmag);
             s = fe_to_double(S);
@@ -703,9 +734,10 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
             wi *= inv;
             dr = fe_to_double(fe_div(dcr, S));
             di = fe_to_double(fe_div(dci, S));
+            keep = false;
         }
-        double dzmag2 = s * s * (wr * wr + wi * wi);
-        if (zrad < 1e-8 || zrad < dzmag2 || (!per && m >= reflen)) {
+        double dzmag2 = s * s * (keep ? wmag2 : wr * wr + wi * wi);
+        if (d_abs_less(zrad, 1e-8) || d_abs_less(zrad, dzmag2) || (!per && m >= reflen)) { // zrad, dzmag2 >= +0 or NaN
             FE Xmr = m ? Zfe[rm].re : fe_make(0.0, 0);
             FE Xmi = m ? Zfe[rm].im : fe_make(0.0, 0);
             FE Swr = fe_mul_d(S, wr), Swi = fe_mul_d(S, wi);
@@ -727,8 +759,10 @@ __device__ PixOut pixel_fe(const DeviceFrame& f, const FeParams& p, FE dcr, FE d
                 }
                 m = 0;
                 rm = -1;
+                keep = false;
             }
         }
+        if (keep) wm2_known = wmag2;
     }
     o.value = oc.interior();
     o.state = 2;
