@@ -306,6 +306,67 @@ MBX_HD F32E te_add_f(F32E a, F32E b) {
     return te_norm(te_align_f(a.m, a.e, e) + te_align_f(b.m, b.e, e), e);
 }
 
+// The double-float lane's rare steps in double-float floatexp (df32 mantissa,
+// int exponent), the same operations as the FP32 lane's above at about 48
+// bits: the lane's error estimate covers their roundings (kEps2 per step) like
+// any other step's, and they take no FP64 instruction.
+// FE -> double-float floatexp; the mantissa's 53 bits split on the bit
+// pattern (the top 24 bits exactly, the rest rounded to float).
+MBX_HD TE<df32> te_from_fe_df(FE a) {
+    if (d_is_zero(a.m)) return TE<df32>{df32(0.0f), 0};
+    const uint64_t b = dbits(a.m);
+    const int ex = (int)((b >> 52) & 0x7ff); // 1022 for a normalised mantissa in [0.5, 1)
+    const unsigned sg = (unsigned)(b >> 63) << 31;
+    const float hi = bitsf(sg | (126u << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+    const float lo = (float)(unsigned)(b & 0x1fffffffu) * 0x1p-53f;
+    const df32 m = df_fast_two_sum(hi, sg ? -lo : lo);
+    return TE<df32>{m, (int)a.e + ex - 1022};
+}
+MBX_HD df32 te_align_df(df32 m, int me, int e) { // m 2^me in units of 2^e
+    const int d = me - e;
+    if (m.hi == 0.0f || d < -60) return df32(0.0f);
+    return ldexp_ftz(m, d);
+}
+MBX_HD TE<df32> te_add_df(TE<df32> a, TE<df32> b) {
+    if (a.m.hi == 0.0f) return b;
+    if (b.m.hi == 0.0f) return a;
+    const int e = imax(a.e, b.e);
+    return te_norm(te_align_df(a.m, a.e, e) + te_align_df(b.m, b.e, e), e);
+}
+MBX_HD void exact_step_df(TE<df32> Xr, TE<df32> Xi, TE<df32> dcr, TE<df32> dci, TE<df32>& S, df32& wr, df32& wi) {
+    const df32 sm = S.m, sm2 = sm * sm;
+    const int se = S.e;
+    int e = INT_MIN;
+    const bool has_w = wr.hi != 0.0f || wi.hi != 0.0f;
+    if (has_w && Xr.m.hi != 0.0f) e = imax(e, Xr.e + se);
+    if (has_w && Xi.m.hi != 0.0f) e = imax(e, Xi.e + se);
+    if (has_w) e = imax(e, se + se);
+    if (dcr.m.hi != 0.0f) e = imax(e, dcr.e);
+    if (dci.m.hi != 0.0f) e = imax(e, dci.e);
+    if (e == INT_MIN) {
+        S = TE<df32>{df32(0.5f), 1};
+        wr = wi = df32(0.0f);
+        return;
+    }
+    const df32 xs_r = te_align_df(Xr.m * sm, Xr.e + se, e);
+    const df32 xs_i = te_align_df(Xi.m * sm, Xi.e + se, e);
+    const df32 s2 = te_align_df(sm2, se + se, e);
+    const df32 cr = te_align_df(dcr.m, dcr.e, e);
+    const df32 ci = te_align_df(dci.m, dci.e, e);
+    const df32 two(2.0f);
+    const df32 nr = two * (xs_r * wr - xs_i * wi) + s2 * (wr * wr - wi * wi) + cr;
+    const df32 ni = two * (xs_r * wi + xs_i * wr) + two * s2 * wr * wi + ci;
+    const df32 mag = tsqrt(nr * nr + ni * ni);
+    if (mag.hi == 0.0f) {
+        S = TE<df32>{df32(0.5f), 1};
+        wr = wi = df32(0.0f);
+        return;
+    }
+    S = te_norm(mag, e);
+    wr = nr / mag;
+    wi = ni / mag;
+}
+
 // Floatexp copy of the FP64 BLA table: A and B as mantissa pairs with one
 // exponent each, the radius^2 as mantissa + exponent. Built once per reference
 // from the FP64 table (k_bla_to_lane).
@@ -1252,7 +1313,7 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
         // normal number, where dz^2 can be as large as dc (z ~ sqrt(minibrot
         // size) at a nucleus pass).
         const bool tiny = (L.m == 0 && !(L.s >= R::kMinS)) ||
-                          (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && (Zfe[L.rm].re.m != 0.0 || Zfe[L.rm].im.m != 0.0));
+                          (L.m != 0 && tabs(L.Xc.x) < R::kTinyX && tabs(L.Xc.y) < R::kTinyX && !(d_is_zero(Zfe[L.rm].re.m) && d_is_zero(Zfe[L.rm].im.m)));
         if (deriv) { // J' = 2 z J + 1 with the pre-step z (mp.cpp:3436-3441, 3478-3497)
             if (!tiny) {
                 lane_j_advance(L);
@@ -1283,6 +1344,27 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 const int ez = zr.m == 0.0f ? zi.e : (zi.m == 0.0f ? zr.e : imax(zr.e, zi.e));
                 const float mr = te_align_f(zr.m, zr.e, ez), mi = te_align_f(zi.m, zi.e, ez);
                 const float q = S.m == 0.0f ? 0.0f : S0.m / S.m;
+                const float amp = ldexp_ftz(4.0f * (mr * mr + mi * mi) * q * q, imax(-300, imin(300, 2 * ez + 2 * (S0.e - S.e))));
+                L.err2 = fminf(amp * L.err2, 3e38f) + R::kEps2;
+            }
+            L.S = S;
+            L.wr = wr;
+            L.wi = wi;
+            lane_refresh(L);
+        } else if constexpr (std::is_same<T, df32>::value) {
+            ++n_exact;
+            const TE<df32> S0 = L.S;
+            const TE<df32> zero{df32(0.0f), 0};
+            const TE<df32> Xr = L.m ? te_from_fe_df(Zfe[L.rm].re) : zero, Xi = L.m ? te_from_fe_df(Zfe[L.rm].im) : zero;
+            TE<df32> S = S0;
+            df32 wr = L.wr, wi = L.wi;
+            exact_step_df(Xr, Xi, te_norm(L.dcm.x, L.dce), te_norm(L.dcm.y, L.dce), S, wr, wi);
+            if (R::kTrackError) {
+                // error carried into the new units: |2 z|^2 (S0 / S)^2 err2, z = X + S0 w
+                const TE<df32> zr = te_add_df(Xr, te_norm(S0.m * L.wr, S0.e)), zi = te_add_df(Xi, te_norm(S0.m * L.wi, S0.e));
+                const int ez = zr.m.hi == 0.0f ? zi.e : (zi.m.hi == 0.0f ? zr.e : imax(zr.e, zi.e));
+                const float mr = te_align_df(zr.m, zr.e, ez).hi, mi = te_align_df(zi.m, zi.e, ez).hi;
+                const float q = S.m.hi == 0.0f ? 0.0f : S0.m.hi / S.m.hi;
                 const float amp = ldexp_ftz(4.0f * (mr * mr + mi * mi) * q * q, imax(-300, imin(300, 2 * ez + 2 * (S0.e - S.e))));
                 L.err2 = fminf(amp * L.err2, 3e38f) + R::kEps2;
             }
@@ -1459,6 +1541,45 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 L.rm = -1;
                 L.Xc = R::make2(T(0), T(0));
                 ++n_rebase;
+            }
+        } else if (decide == 2 && std::is_same<T, df32>::value) {
+            if constexpr (std::is_same<T, df32>::value) {
+                // the decision and the new delta in double-float floatexp, as
+                // the FP32 lane's above
+                ++n_ferebase;
+                const TE<df32> zero{df32(0.0f), 0};
+                const TE<df32> Xr = L.m ? te_from_fe_df(Zfe[L.rm].re) : zero, Xi = L.m ? te_from_fe_df(Zfe[L.rm].im) : zero;
+                const df32 Sm = L.S.m;
+                const TE<df32> zr = te_add_df(Xr, te_norm(Sm * L.wr, L.S.e)), zi = te_add_df(Xi, te_norm(Sm * L.wi, L.S.e));
+                const int ez = zr.m.hi == 0.0f ? zi.e : (zi.m.hi == 0.0f ? zr.e : imax(zr.e, zi.e));
+                const df32 mr = te_align_df(zr.m, zr.e, ez), mi = te_align_df(zi.m, zi.e, ez);
+                const df32 mz = tsqrt(mr * mr + mi * mi);
+                const TE<df32> zn = te_norm(mz, ez), dn = te_norm(tabs(Sm) * tsqrt(L.wr * L.wr + L.wi * L.wi), L.S.e);
+                const bool smaller = zn.m.hi == 0.0f ? dn.m.hi != 0.0f : (dn.m.hi != 0.0f && (zn.e < dn.e || (zn.e == dn.e && zn.m < dn.m)));
+                if ((!per && L.m >= reflen) || smaller) {
+                    if (mz.hi == 0.0f) {
+                        L.wr = L.wi = df32(0.0f);
+                    } else {
+                        const float wrf = L.wr.hi, wif = L.wi.hi, smf = Sm.hi, mzf = mz.hi;
+                        L.S = zn;
+                        L.wr = mr / mz;
+                        L.wi = mi / mz;
+                        lane_refresh(L);
+                        if (R::kTrackError) {
+                            // plus the roundings of X + dz, relative to |z|:
+                            // (|X|^2 + |dz|^2) / |z|^2 times the per-step variance
+                            const int ex = Xr.m.hi == 0.0f ? Xi.e : (Xi.m.hi == 0.0f ? Xr.e : imax(Xr.e, Xi.e));
+                            const float ar = te_align_df(Xr.m, Xr.e, ex).hi, ai = te_align_df(Xi.m, Xi.e, ex).hi;
+                            const float cx = (Xr.m.hi == 0.0f && Xi.m.hi == 0.0f) ? 0.0f : ldexp_ftz((ar * ar + ai * ai) / (mzf * mzf), imax(-300, imin(300, 2 * (ex - ez))));
+                            const float cd = ldexp_ftz(smf * smf * (wrf * wrf + wif * wif) / (mzf * mzf), imax(-300, imin(300, 2 * (S0.e - ez))));
+                            L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2 * (1.0f + fminf(cx + cd, 1e30f));
+                        }
+                    }
+                    L.m = 0;
+                    L.rm = -1;
+                    L.Xc = R::make2(T(0), T(0));
+                    ++n_rebase;
+                }
             }
         } else if (decide == 2) {
             ++n_ferebase;
