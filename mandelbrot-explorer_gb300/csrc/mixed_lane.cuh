@@ -306,10 +306,13 @@ MBX_HD F32E te_add_f(F32E a, F32E b) {
     return te_norm(te_align_f(a.m, a.e, e) + te_align_f(b.m, b.e, e), e);
 }
 
-// The double-float lane's rare steps in double-float floatexp (df32 mantissa,
-// int exponent), the same operations as the FP32 lane's above at about 48
-// bits: the lane's error estimate covers their roundings (kEps2 per step) like
-// any other step's, and they take no FP64 instruction.
+// The double-float lane's orbit-entry steps in double-float floatexp (df32
+// mantissa, int exponent), the same operations as the FP32 lane's above at
+// about 48 bits: the lane's error estimate covers their roundings (kEps2 per
+// step) like any other step's, and they take no FP64 instruction. (Its
+// floatexp rebase decisions stay in FP64: in double-float floatexp their
+// rounding of X + dz relative to |z| grows the estimate at every rebase, and
+// the DE frames' double-float tier ran 1.3-1.8x longer.)
 // FE -> double-float floatexp; the mantissa's 53 bits split on the bit
 // pattern (the top 24 bits exactly, the rest rounded to float).
 MBX_HD TE<df32> te_from_fe_df(FE a) {
@@ -1541,45 +1544,6 @@ MBX_HDF int lane_run(Lane<T>& L, int budget, const DeviceFrame& f, const MixedPa
                 L.rm = -1;
                 L.Xc = R::make2(T(0), T(0));
                 ++n_rebase;
-            }
-        } else if (decide == 2 && std::is_same<T, df32>::value) {
-            if constexpr (std::is_same<T, df32>::value) {
-                // the decision and the new delta in double-float floatexp, as
-                // the FP32 lane's above
-                ++n_ferebase;
-                const TE<df32> zero{df32(0.0f), 0};
-                const TE<df32> Xr = L.m ? te_from_fe_df(Zfe[L.rm].re) : zero, Xi = L.m ? te_from_fe_df(Zfe[L.rm].im) : zero;
-                const df32 Sm = L.S.m;
-                const TE<df32> zr = te_add_df(Xr, te_norm(Sm * L.wr, L.S.e)), zi = te_add_df(Xi, te_norm(Sm * L.wi, L.S.e));
-                const int ez = zr.m.hi == 0.0f ? zi.e : (zi.m.hi == 0.0f ? zr.e : imax(zr.e, zi.e));
-                const df32 mr = te_align_df(zr.m, zr.e, ez), mi = te_align_df(zi.m, zi.e, ez);
-                const df32 mz = tsqrt(mr * mr + mi * mi);
-                const TE<df32> zn = te_norm(mz, ez), dn = te_norm(tabs(Sm) * tsqrt(L.wr * L.wr + L.wi * L.wi), L.S.e);
-                const bool smaller = zn.m.hi == 0.0f ? dn.m.hi != 0.0f : (dn.m.hi != 0.0f && (zn.e < dn.e || (zn.e == dn.e && zn.m < dn.m)));
-                if ((!per && L.m >= reflen) || smaller) {
-                    if (mz.hi == 0.0f) {
-                        L.wr = L.wi = df32(0.0f);
-                    } else {
-                        const float wrf = L.wr.hi, wif = L.wi.hi, smf = Sm.hi, mzf = mz.hi;
-                        L.S = zn;
-                        L.wr = mr / mz;
-                        L.wi = mi / mz;
-                        lane_refresh(L);
-                        if (R::kTrackError) {
-                            // plus the roundings of X + dz, relative to |z|:
-                            // (|X|^2 + |dz|^2) / |z|^2 times the per-step variance
-                            const int ex = Xr.m.hi == 0.0f ? Xi.e : (Xi.m.hi == 0.0f ? Xr.e : imax(Xr.e, Xi.e));
-                            const float ar = te_align_df(Xr.m, Xr.e, ex).hi, ai = te_align_df(Xi.m, Xi.e, ex).hi;
-                            const float cx = (Xr.m.hi == 0.0f && Xi.m.hi == 0.0f) ? 0.0f : ldexp_ftz((ar * ar + ai * ai) / (mzf * mzf), imax(-300, imin(300, 2 * (ex - ez))));
-                            const float cd = ldexp_ftz(smf * smf * (wrf * wrf + wif * wif) / (mzf * mzf), imax(-300, imin(300, 2 * (S0.e - ez))));
-                            L.err2 = L.err2 * lane_scale_ratio2(S0, L.S) + R::kEps2 * (1.0f + fminf(cx + cd, 1e30f));
-                        }
-                    }
-                    L.m = 0;
-                    L.rm = -1;
-                    L.Xc = R::make2(T(0), T(0));
-                    ++n_rebase;
-                }
             }
         } else if (decide == 2) {
             ++n_ferebase;
