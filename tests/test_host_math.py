@@ -36,6 +36,31 @@ int main() {
         double zr = z.real(), zi = z.imag();
         if (std::isfinite(zr) && std::isfinite(zi) && (dbits(zr) != dbits(q.re) || dbits(zi) != dbits(q.im))) ++bad;
     }
+    // the exact loop's tests on bit patterns (d_is_zero, d_abs_less, d_eq,
+    // d_le_zero) and its doubling (d_twice) give the IEEE results, NaN,
+    // infinities, signed zeros and subnormals included
+    const double sp[] = {0.0, -0.0, 1.0, -1.0, 5e-324, -5e-324, 2.2250738585072014e-308, 8.98846567431158e307, 1.7976931348623157e308,
+                         -1.7976931348623157e308, INFINITY, -INFINITY, NAN, -NAN, 1e-8, 1e16, 1e-16, 0.5, 0.9999999999999999};
+    std::uniform_int_distribution<uint64_t> ub;
+    for (long i = 0; i < 4000000; ++i) {
+        double a, b;
+        if (i < 19 * 19) {
+            a = sp[i / 19];
+            b = sp[i % 19];
+        } else {
+            uint64_t x = ub(g), y = ub(g);
+            if (i & 1) y = x ^ (ub(g) & 0xff); // near neighbours
+            a = bitsd(x);
+            b = bitsd(y);
+            if (i & 2) b = std::fabs(b);
+        }
+        if (d_is_zero(a) != (a == 0.0)) ++bad;
+        if (d_abs_less(a, b) != (std::fabs(a) < std::fabs(b))) ++bad;
+        if (d_eq(a, b) != (a == b)) ++bad;
+        if (d_le_zero(a) != (a <= 0.0)) ++bad;
+        const double t = a + a;
+        if (!std::isnan(a) && dbits(d_twice(a)) != dbits(t)) ++bad;
+    }
     LibcRand r;
     r.seed(1);
     srand(1);
