@@ -84,6 +84,49 @@ def test_floatexp_complex_and_rand_match_libc():
         assert out.returncode == 0, out.stdout + out.stderr
 
 
+SPLIT_PROGRAM = r"""
+#include "mixed_lane.cuh"
+#include <cmath>
+#include <cstdio>
+#include <random>
+using namespace mbx;
+int main() {
+    std::mt19937_64 g(7);
+    std::uniform_real_distribution<double> u(0.5, 1.0);
+    long bad = 0;
+    for (long i = 0; i < 2000000; ++i) {
+        const double m = u(g) * ((i & 1) ? -1.0 : 1.0);
+        const int e = (int)(g() % 2001) - 1000;
+        const TE<df32> t = te_from_fe_df(fe_make(m, e));
+        const double v = ((double)t.m.hi + (double)t.m.lo) * std::ldexp(1.0, t.e - e);
+        if (std::fabs(v - m) > std::ldexp(std::fabs(m), -48)) ++bad;               // the pair's 48 bits
+        if (std::fabs(t.m.lo) > std::ldexp(std::fabs(t.m.hi), -24)) ++bad;         // a normalised pair
+        if (std::fabs(t.m.hi) < 0.5f || std::fabs(t.m.hi) > 1.0f) ++bad;           // mantissa range
+    }
+    if (te_from_fe_df(fe_make(0.0, 7)).m.hi != 0.0f) ++bad;
+    printf("%ld\n", bad);
+    return bad != 0;
+}
+"""
+
+
+def test_floatexp_to_double_float_split():
+    """The double-float lane's orbit-entry steps read FE orbit entries as
+    double-float floatexp (mixed_lane.cuh te_from_fe_df: the 53-bit mantissa
+    split on its bit pattern, no FP64 instruction): the pair must hold the
+    mantissa to the double-float's 48 bits, normalised, with the exponent
+    carried."""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.cpp")
+        exe = os.path.join(d, "t")
+        open(src, "w").write(SPLIT_PROGRAM)
+        csrc = os.path.join(PKG, "csrc")
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wno-deprecated-declarations", "-I" + csrc, "-I/usr/local/cuda/include", src, "-o", exe]
+        subprocess.check_call(cmd)
+        out = subprocess.run([exe], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+
+
 def test_threaded_nucleus_search_matches_serial_oracle():
     """mbx_find_nucleus runs the period search and the Newton orbit on three
     threads between 1000 and 1600/2000 bits (ring-buffered recurrences), and
