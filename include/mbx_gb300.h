@@ -21,9 +21,9 @@ extern "C" {
  * (src/engine/mandel_perturbation.h:30-49). Other bits are rejected. */
 #define MBX_SUPER_SAMPLING 1
 #define MBX_EXTERIOR_DIST_EST 2
-#define MBX_STRIPE_AVERAGE 8 /* value = stripe average over the last 256 iterations (src/engine/orbit_coloring.h:21-95); sub 1, exact form */
+#define MBX_STRIPE_AVERAGE 8 /* value = stripe average over the last 256 iterations (src/engine/orbit_coloring.h:21-95); exact form; with MBX_SUPER_SAMPLING the set boundary is resampled (mp.cpp:1810-1826) */
 #define MBX_NORMAL_MAP 16 /* value = smooth iteration; normal buffer = arg(z) - arg(dz/dc) (mp.cpp:375-378, 2489-2492, 3512-3515) */
-#define MBX_ORBIT_TRAP 32 /* value = 0.17 (-log10 trap distance) + 0.025 mu (orbit_coloring.h:97-132); interior samples carry it too; sub 1, exact form */
+#define MBX_ORBIT_TRAP 32 /* value = 0.17 (-log10 trap distance) + 0.025 mu (orbit_coloring.h:97-132); interior samples carry it too; exact form; with MBX_SUPER_SAMPLING pixels whose trap colour changes by more than 3 palette entries are resampled (mp.cpp:1827-1838) */
 #define MBX_DE_OVERLAY 64
 
 /* What a request renders (ComputeMode, src/engine/compute_backend.h:18). */

@@ -44,8 +44,6 @@ int validate(const mbx_request* r, std::string& why) {
         why = "Julia takes sub 1, the fixed c and coloring 0 or MBX_EXTERIOR_DIST_EST";
     else if ((r->coloring_method & ~(MBX_SUPER_SAMPLING | MBX_EXTERIOR_DIST_EST | MBX_STRIPE_AVERAGE | MBX_NORMAL_MAP | MBX_ORBIT_TRAP | MBX_DE_OVERLAY)) != 0)
         why = "unsupported coloring_method bits";
-    else if ((r->coloring_method & (MBX_STRIPE_AVERAGE | MBX_ORBIT_TRAP)) && (r->sub != 1 || (r->coloring_method & MBX_SUPER_SAMPLING)))
-        why = "stripe average and orbit traps are rendered at sub 1 (no adaptive supersampling)";
     else if (r->precision_mode != MBX_PRECISION_EXACT && r->precision_mode != MBX_PRECISION_MIXED) why = "unknown precision_mode";
     else if (!(r->bailout >= 0.0) || r->bailout > 1e18) why = "bailout must be in [0, 1e18]";
     else if ((long long)r->width * r->sub * r->height * r->sub > (1ll << 31) - 1) why = "frame too large";

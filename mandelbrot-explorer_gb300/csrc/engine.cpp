@@ -2296,7 +2296,14 @@ int Engine::glitch_loop(std::vector<uint64_t>& pending, int& ref_it, bool have, 
 int Engine::supersample(int ref_it) {
     if (!ensure(dflags_, (size_t)W_ * H_)) return MBX_E_NOMEM;
     const double thresh = std::log((double)MXIT_) / 8.0;
-    cudaError_t e = launch_ss_flags(out_iter_, W_, H_, SUB_, (cm_ & 2) ? 1 : 0, thresh, dflags_.p, st_);
+    // EDE: the set boundary; the stripe average: the boundary (palette steps 0);
+    // orbit traps: the boundary or more than 3 palette entries per pixel, at the
+    // palette density 60 the compute backend leaves (mp.cpp:1810-1838)
+    const double density = 60.0;
+    const int mode = (cm_ & 2) ? kSsEde : (cm_ & 8) ? kSsStripe : (cm_ & 32) ? kSsTrap : kSsIterations;
+    const double gain = mode == kSsStripe ? density * (2048.0 / 20.0) : density / 60.0 * 2048.0;
+    const double steps = mode == kSsStripe ? 0.0 : 3.0;
+    cudaError_t e = launch_ss_flags(out_iter_, W_, H_, SUB_, mode, thresh, gain, steps, dflags_.p, st_);
     ++stats_.kernel_launches;
     if (e != cudaSuccess) return fail_cuda("ss flags", e);
     std::vector<uint8_t> flags((size_t)W_ * H_);
@@ -2466,6 +2473,10 @@ int Engine::shallow_samples(const std::vector<uint64_t>& samples) {
     p.g = geom();
     p.g.deovl = 0; // sub-samples carry the smooth/EDE value only (mp.cpp:1936-1967)
     p.g.normal = 0;
+    // Up to 128 sub-samples per pixel take the reference's lane kernel, which
+    // has no stripe average (a SAC frame's sub-samples take the scalar path)
+    // and no orbit traps (a trap frame's sub-samples get the smooth count).
+    if (!(cm_ & 8) && (cm_ & 32) && SUB_ * SUB_ <= 128) p.g.oc = 0;
     p.c0r = mpf_ld(c0_re_);
     p.c0i = mpf_ld(c0_im_);
     p.dx = mpf_ld(dx_);

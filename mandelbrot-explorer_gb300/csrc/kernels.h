@@ -213,7 +213,9 @@ cudaError_t launch_julia(const DeviceFrame& f, const JuliaParams& p, int blocks,
 cudaError_t launch_bla_build(const double2* Z, const double2* D, int reflen, double eps, double dcmax, bool ede,
                              double* r2, double4* ab, double4* ce, const int* off, const int* size, int nlev,
                              unsigned long long* rmax2_bits, cudaStream_t st);
-cudaError_t launch_ss_flags(const float* iter, int W, int H, int sub, int ede, double thresh, uint8_t* flags, cudaStream_t st);
+// adaptive-SS selection modes (k_ss_flags)
+constexpr int kSsIterations = 0, kSsEde = 1, kSsStripe = 2, kSsTrap = 3;
+cudaError_t launch_ss_flags(const float* iter, int W, int H, int sub, int mode, double thresh, double gain, double steps, uint8_t* flags, cudaStream_t st);
 
 // Mixed-precision (FP32 floatexp) pass (kernels_mixed.cu).
 struct MixedParams {

@@ -1192,13 +1192,19 @@ __global__ void k_bla_merge(double dcmax, int ede, double* r2, double4* ab, doub
 
 // ---------------------------------------------------------------------------
 // Adaptive-SS flags over the base samples (mp.cpp:1838-1884).
-__global__ void k_ss_flags(const float* iter, int W, int H, int sub, int ede, double thresh, uint8_t* flags) {
+// Adaptive-SS selection (mp.cpp:1796-1879). mode: kSsIterations (the
+// iteration difference against thresh), kSsEde (a sign change: the set
+// boundary), kSsStripe / kSsTrap (the stripe average and orbit traps store a
+// value, not a count: the set boundary, or a colour change of more than
+// `steps` palette entries per pixel, `gain` entries per unit of value; the
+// stripe average's steps default to 0, the boundary only).
+__global__ void k_ss_flags(const float* iter, int W, int H, int sub, int mode, double thresh, double gain, double steps, uint8_t* flags) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= W * H) return;
     int i = q / W, j = q % W;
     auto at = [&](int r, int c) { return iter[(r * sub + sub / 2) * W * sub + (c * sub + sub / 2)]; };
     bool need = false;
-    if (ede) {
+    if (mode == kSsEde) {
         float cv = at(i, j);
         for (int xi = -1; xi <= 1 && !need; ++xi)
             for (int yi = -1; yi <= 1; ++yi) {
@@ -1212,13 +1218,23 @@ __global__ void k_ss_flags(const float* iter, int W, int H, int sub, int ede, do
     } else {
         float cv = at(i, j);
         float diff = 0;
+        bool boundary = false;
         for (int xi = -1; xi <= 1; ++xi)
             for (int yi = -1; yi <= 1; ++yi) {
                 if (xi == 0 && yi == 0) continue;
                 int ny = i + yi, nx = j + xi;
-                if (nx >= 0 && nx < W && ny >= 0 && ny < H) diff = fmaxf(diff, fabsf(cv - at(ny, nx)));
+                if (nx >= 0 && nx < W && ny >= 0 && ny < H) {
+                    const float nv = at(ny, nx);
+                    diff = fmaxf(diff, fabsf(cv - nv));
+                    if (cv * nv < 0) boundary = true; // interior / exterior edge
+                }
             }
-        need = log((double)diff) > thresh;
+        if (mode == kSsStripe)
+            need = boundary || (steps > 0 && diff * gain > steps);
+        else if (mode == kSsTrap)
+            need = boundary || (diff * gain > steps);
+        else
+            need = log((double)diff) > thresh;
     }
     flags[q] = need ? 1 : 0;
 }
@@ -1284,9 +1300,9 @@ cudaError_t launch_bla_build(const double2* Z, const double2* D, int reflen, dou
     }
     return cudaGetLastError();
 }
-cudaError_t launch_ss_flags(const float* iter, int W, int H, int sub, int ede, double thresh, uint8_t* flags, cudaStream_t st) {
+cudaError_t launch_ss_flags(const float* iter, int W, int H, int sub, int mode, double thresh, double gain, double steps, uint8_t* flags, cudaStream_t st) {
     int n = W * H;
-    k_ss_flags<<<(n + 255) / 256, 256, 0, st>>>(iter, W, H, sub, ede, thresh, flags);
+    k_ss_flags<<<(n + 255) / 256, 256, 0, st>>>(iter, W, H, sub, mode, thresh, gain, steps, flags);
     return cudaGetLastError();
 }
 

@@ -401,6 +401,9 @@ struct Opts {
     int bigfixed = -1; // MANDEL_BIGFIXED
     int fused = 1;     // MANDEL_FUSED_PERTURB
     double ss_k = 8.0; // MANDEL_SS_K
+    double sac_ss_steps = 0.0;  // MANDEL_SAC_SS_STEPS (0: the set boundary only)
+    double trap_ss_steps = 3.0; // MANDEL_TRAP_SS_STEPS
+    float ss_density = 60.0f;   // Mandel::_ss_density (setDensity; the compute backend leaves the default)
 };
 
 struct Pix {
@@ -2307,6 +2310,12 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
     // Adaptive supersampling (mp.cpp:1796-2006).
     std::vector<std::array<int, 2>> v;
     const double ss_thresh = std::log((double)mxit) / opt.ss_k;
+    // the stripe average and the orbit traps store a value, not an iteration
+    // count: the set boundary (a sign change) and, for traps, a colour change of
+    // more than trap_ss_steps palette entries per pixel (mp.cpp:1810-1838, 1864-1870)
+    const bool sac = (cm & CM_SAC) != 0, trap = (cm & CM_TRAP) != 0;
+    const double sac_gain = (double)opt.ss_density * (2048.0 / 20.0);
+    const double trap_gain = (double)opt.ss_density / 60.0 * 2048.0;
     for (int i = 0; i < H; ++i) {
         for (int j = 0; j < W; ++j) {
             bool need = false;
@@ -2323,13 +2332,23 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
             } else {
                 float cv = iter_[idx(Pix{{i, j, 0, 0}})];
                 float diff = 0;
+                bool boundary = false;
                 for (int xi = -1; xi <= 1; ++xi)
                     for (int yi = -1; yi <= 1; ++yi) {
                         if (xi == 0 && yi == 0) continue;
                         int ny = i + yi, nx = j + xi;
-                        if (nx >= 0 && nx < W && ny >= 0 && ny < H) diff = std::max(diff, std::abs(cv - iter_[idx(Pix{{ny, nx, 0, 0}})]));
+                        if (nx >= 0 && nx < W && ny >= 0 && ny < H) {
+                            const float nv = iter_[idx(Pix{{ny, nx, 0, 0}})];
+                            diff = std::max(diff, std::abs(cv - nv));
+                            if ((sac || trap) && cv * nv < 0) boundary = true;
+                        }
                     }
-                need = (std::log((double)diff) > ss_thresh); // log(float) resolves to ::log(double) in the reference build
+                if (sac)
+                    need = boundary || (opt.sac_ss_steps > 0 && diff * sac_gain > opt.sac_ss_steps);
+                else if (trap)
+                    need = boundary || (diff * trap_gain > opt.trap_ss_steps);
+                else
+                    need = (std::log((double)diff) > ss_thresh); // log(float) resolves to ::log(double) in the reference build
             }
             if (need) v.push_back({i, j});
         }
@@ -2344,10 +2363,14 @@ void Engine::compute(mpf_srcptr c_re, mpf_srcptr c_im, mpf_srcptr scale, int mxi
                     if (xi == 0 && yi == 0) continue;
                     double cr = c0r + dxf * v[q][1] + dxf * xi / SUB;
                     double ci = c0i + dyf * v[q][0] + dyf * yi / SUB;
-                    // sub^2 <= 128 takes the lane-refill kernel (float result), larger
-                    // sub the scalar floatPointCompute (double result) (mp.cpp:1936-1967).
+                    // sub^2 <= 128 takes the lane-refill kernel (float result; it has
+                    // no stripe average, so SAC frames take the scalar path, and no
+                    // orbit traps, so a trap frame's subsamples get the smooth count),
+                    // larger sub the scalar floatPointCompute (double result)
+                    // (mp.cpp:1931-1967).
                     int nn = -1;
-                    double it = (SUB * SUB <= 128) ? (double)shallowSimd(cr, ci, mxit, cm, &nn) : floatPoint(cr, ci, mxit, cm & CM_EDE, nullptr, &nn);
+                    const bool simd = (SUB * SUB <= 128) && !sac;
+                    double it = simd ? (double)shallowSimd(cr, ci, mxit, cm, &nn) : floatPoint(cr, ci, mxit, cm & (CM_EDE | CM_SAC | CM_TRAP), nullptr, &nn);
                     if (ede && it >= 0) it /= dxf;
                     setPixel(Pix{{v[q][0], v[q][1], yi, xi}}, (float)it, nn);
                 }
