@@ -177,7 +177,7 @@ def profile_run(args, vlist):
         times = []
         for k in range(args.warmup + args.steps):
             t = time.perf_counter()
-            req, st = render(be, mbx, v, mbx.PRECISION_MIXED, reuse=True, width=args.width, height=args.height)
+            req, st = render(be, mbx, v, mbx.PRECISION_EXACT if args.profile_exact else mbx.PRECISION_MIXED, reuse=True, width=args.width, height=args.height)
             # the render tool's image epilogue on the frame (host values, RGB back)
             be.colorize(req.iterations, args.width, args.height, mbx.ColorParams())
             if k >= args.warmup:
@@ -205,6 +205,7 @@ def main():
     ap.add_argument("--plain-sample", default="full", help="plain FP64 GPU sample size (same views), WxH or 'full' (the frames' own size)")
     ap.add_argument("--profile", default=None, help="comma-separated view labels (e.g. 1e-300): render (and colour) only those, default launch shape, no baselines (for ncu captures)")
     ap.add_argument("--profile-batch", action="store_true", help="with --profile: render the views as one batch with the learned ordering training")
+    ap.add_argument("--profile-exact", action="store_true", help="with --profile: render the views in the exact form (MBX_PRECISION_EXACT)")
     ap.add_argument("--profile-c4", type=int, default=0, help="render N tiles of the learned-scheduling image as one batch with the model training on it (for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
